@@ -1,0 +1,136 @@
+/*
+ * umwm_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the UMWM
+ * per-time-step path: source terms and their exponential integration,
+ * upwind propagation, refraction, wind stress and Stokes drift.
+ *
+ * Plain pointers and sizes only.  Every call returns UMWM_OK (0) or one of
+ * the UMWM_ERR_* codes; umwm_gpu_last_error() returns the message of the
+ * last failure.  The library never calls exit().
+ *
+ * One process-wide model, like the reference's module-global memory pool
+ * (umwm_module.F90:98-207).  Calls are not re-entrant; use one host thread.
+ *
+ * Arrays follow the reference's Fortran layouts, given as flat C arrays:
+ *   2-d fields (mm, nm)      : m fastest, index (m-1) + (n-1)*mm
+ *   spectrum F(om, pm, im)   : o fastest, then p, then the wet index i
+ *   wet-point fields (im)    : unrolled wet index i = 1..im, at offset i-1
+ *
+ * Inputs the reference reads from netCDF files are staged in memory under
+ * the same names and time keys (there is no netCDF library on this
+ * platform); umwm_gpu_initialize / umwm_gpu_run read them where the
+ * reference opens the file.
+ */
+#ifndef UMWM_GPU_H
+#define UMWM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UMWM_OK 0
+#define UMWM_ERR_NAMELIST 1    /* bad or missing namelist value (umwm_init.F90:94-185) */
+#define UMWM_ERR_INPUT 2       /* staged input missing or mis-sized (stands in for nc_check, umwm_io.F90:904-915) */
+#define UMWM_ERR_CUDA 3        /* a CUDA call failed */
+#define UMWM_ERR_NONFINITE 4   /* the finite-state check found NaN/Inf in the state */
+#define UMWM_ERR_TIMEOUT 5     /* a bounded device-side wait gave up */
+#define UMWM_ERR_STATE 6       /* call out of order (e.g. run before initialize) */
+#define UMWM_ERR_ARG 7         /* bad argument (null pointer, wrong size, unknown name) */
+#define UMWM_ERR_UNSUPPORTED 8 /* configuration outside what this build supports */
+
+/* ---- input staging (stand-ins for the files the reference opens) ------- */
+
+/* input/umwm.gridtopo variables 'lon', 'lat' (gridFromFile) and 'z'
+ * (topoFromFile); replaces umwm_init.F90:397-427 and :541-546. */
+int umwm_gpu_put_gridtopo(const char* var, const float* field_mn, int mm, int nm);
+
+/* namelists/exclude.nml seed points (m, n) for fillLakes; replaces
+ * umwm_init.F90:640-651.  mn holds npairs pairs. */
+int umwm_gpu_put_exclude(const int* mn, int npairs);
+
+/* input/umwmin_<time>.nc variable 'uw','vw','uc','vc','rhoa','rhow' or
+ * 'fice' for the 19-character time key 'YYYY-MM-DD hh:mm:ss' (or with '_'
+ * between date and time); replaces the reads of umwm_io.F90:13-93. */
+int umwm_gpu_put_forcing(const char* time19, const char* var, const float* field_mn, int mm, int nm);
+
+/* restart/umwmrst_<time>.nc variables 'F' (om*pm*im floats) and 'ust'
+ * (im floats); replaces restart_read, umwm_restart.F90:19-56. */
+int umwm_gpu_put_restart(const char* time19, const float* F, long nF, const float* ust, long nust);
+
+/* Drop every staged input. */
+int umwm_gpu_clear_inputs(void);
+
+/* ---- umwm_top entry points --------------------------------------------- */
+
+/* umwm_initialize, umwm_top.F90:7-29.  nml_path NULL means
+ * "namelists/main.nml" relative to the working directory, as the
+ * reference opens it (umwm_init.F90:84). */
+int umwm_gpu_initialize(const char* nml_path);
+
+/* Same as umwm_gpu_initialize with the namelist given as text. */
+int umwm_gpu_initialize_text(const char* nml_text);
+
+/* umwm_run(starttimestr, stoptimestr), umwm_top.F90:32-196.  Times are
+ * 'YYYY-MM-DD hh:mm:ss'. */
+int umwm_gpu_run(const char* start19, const char* stop19);
+
+/* umwm_finalize, umwm_top.F90:199-204: frees every device and host
+ * buffer of the model.  Staged inputs are kept. */
+int umwm_gpu_finalize(void);
+
+/* The host part of umwm_initialize only (namelist, grid, masks,
+ * partition, remap, spectral tables), without touching the GPU, so that
+ * the unrolled grid and tables can be inspected with the getters below. */
+int umwm_gpu_setup_host(const char* nml_text);
+
+/* ---- state and fields ---------------------------------------------------- */
+
+/* dims[0..7] = mm, nm, om, pm, im, imm, lm, substeps-so-far */
+int umwm_gpu_get_dims(int* dims);
+
+/* Spectrum F(om,pm,im) and friction velocity ust(im): what restart_write
+ * stores, umwm_restart.F90:59-154.  Either pointer may be NULL. */
+int umwm_gpu_get_state(float* F, float* ust);
+
+/* Overwrite the spectrum and friction velocity (the restart_read
+ * assignment, umwm_restart.F90:46-49).  Either pointer may be NULL. */
+int umwm_gpu_set_state(const float* F, const float* ust);
+
+/* Copy a named field into out (n floats).  Names are the reference's
+ * variable names: wet-point fields (ht, mwp, mwd, mss, mwl, dwd, dwl, dwp,
+ * dcp0, dcp, dcg0, dcg, momx, momy, cgmxx, cgmxy, cgmyy, ustar, cd, taux,
+ * tauy, taux_form, tauy_form, taux_skin, tauy_skin, taux_diag, tauy_diag,
+ * tailatmx, tailatmy, shelt, fcutoff, physics_time_step, ds, ar, dxn, dxs,
+ * dye, dyw, oneovar, oneovdx, oneovdy), all-point fields over imm (wspd,
+ * wdir, uc, vc, rhoa, rhow, rhorat, fice, d, dx, dy), Stokes drift 'us',
+ * 'vs' (lm*im, level-major), spectral tables (om*im: k, kdk, k3dk, ...;
+ * cp0, cg0 as om*(im+1) with the ghost point first), 'f' (om), 'th' (pm),
+ * 'depth' (lm) and the scalars dts, dta, dtr, dtamin, sumt, cgmax, dth. */
+int umwm_gpu_get_field(const char* name, float* out, long n);
+
+/* Integer fields: mask, ii (mm*nm); mi, ni, iw, ie, is, in, iiw, iie,
+ * iis, iin (imm); oc (im); and scalars im, imm, iip. */
+int umwm_gpu_get_field_i(const char* name, int* out, long n);
+
+/* The per-substep screen line of umwm_top.F90:143-148 (sumt/dtg, dts,
+ * wspd, wdir, swh, mwp, cd*1e3, f(oc) at the print point), 8 doubles per
+ * substep since initialize; returns the number of rows in *rows. */
+int umwm_gpu_get_screen(double* out, long n, long* rows);
+
+/* Options: "verbose" (print the screen lines), "max_substeps" (stop a run
+ * after that many substeps in total; -1 = off), "check_finite" (finite
+ * check of the state after each outer step), "use_graph" (run the inner
+ * loop as one CUDA graph with a device-side while node). */
+int umwm_gpu_set_option(const char* name, double value);
+
+/* Run statistics: "substeps", "gpu_ms" (device time of the last run),
+ * "bin_updates" (wet bins x substeps of the last run), "launches". */
+double umwm_gpu_get_stat(const char* name);
+
+/* Message of the last failure ("" if none). */
+const char* umwm_gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* UMWM_GPU_H */

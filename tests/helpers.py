@@ -1,0 +1,30 @@
+"""Shared helpers of the parity tests: run a Case on the GPU library and on
+the oracle with the same inputs and compare fields."""
+import numpy as np
+
+
+def run_gpu(U, case, max_substeps=-1, start=None, stop=None):
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=case.nml)
+    U.set_option("max_substeps", max_substeps)
+    U.umwm_run(start or case.start, stop or case.stop)
+
+
+def run_oracle(pyoracle, case, prec=32, max_substeps=-1, start=None, stop=None):
+    o = pyoracle.Oracle(case.nml, prec)
+    case.stage(o)
+    o.initialize()
+    o.set_option("max_substeps", max_substeps)
+    o.run(start or case.start, stop or case.stop)
+    return o
+
+
+def rel_err(a, b, floor_frac=1e-6):
+    """Max relative error of a vs b where |b| > floor_frac * max|b|."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    m = np.abs(b) > floor_frac * np.abs(b).max() if b.size and np.abs(b).max() > 0 else np.zeros(b.shape, bool)
+    if not m.any():
+        return float(np.abs(a - b).max()) if a.size else 0.0
+    return float((np.abs(a[m] - b[m]) / np.abs(b[m])).max())

@@ -1,0 +1,10 @@
+"""GB300 (sm_103a) implementation of the UMWM per-time-step path.
+
+The compute path is libumwm_gb300.so (CUDA kernels + C ABI, include/umwm_gpu.h);
+this package is its Python binding, a mirror of the reference's umwm_top
+module, and the synthetic-workload generators.
+"""
+from ._lib import EXPORTS, LIB_PATH, UmwmError, lib  # noqa: F401
+from .top import (clear_inputs, dims, get_field, get_field_i, get_screen, get_state, put_exclude,  # noqa: F401
+                  put_forcing, put_gridtopo, put_restart, set_option, set_state, setup_host, stat,
+                  umwm_finalize, umwm_initialize, umwm_run)

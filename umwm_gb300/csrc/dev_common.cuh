@@ -1,0 +1,71 @@
+// Device helpers shared by the kernel translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "dev.cuh"
+
+namespace umwm {
+
+__device__ __forceinline__ unsigned enc_ord_d(float x) {
+  unsigned u = __float_as_uint(x);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float dec_ord_d(unsigned u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// x^y for x >= 0 through the SFU (lg2/ex2); 0 for x == 0 (as pow does).
+__device__ __forceinline__ float pow_pos(float x, float y) { return exp2f(y * __log2f(x)); }
+
+// sheltering_coare35, umwm_sheltering.F90:49-79
+__device__ __forceinline__ float shelter_coare35(float w) {
+  const float x1 = 15.f, x2 = 33.f, x3 = 60.f, y1 = 0.10f, y2 = 0.09f, y3 = 0.06f;
+  const float intercept = 0.04f, curvature = 0.65f, decay = 1.6f;
+  float slope1 = (y1 - intercept) / x1;
+  float slope2 = (y3 - y2) / (x3 - x2);
+  float c = curvature * (slope2 - slope1) / (x2 - x1);
+  float b = slope1 - 2.f * c * x1;
+  float a = y1 - b * x1 - c * (x1 * x1);
+  float s1 = a + b * x2 + c * (x2 * x2);
+  if (w <= x1) return intercept + slope1 * w;
+  if (w <= x2) return a + b * w + c * (w * w);
+  return s1 * expf(-(w - x2) / (decay * w));
+}
+
+// Per-point inputs of the wind-input source term, sin_d12
+// (umwm_source_functions.F90:16-82).
+struct WindIn {
+  float wspd, uc, vc, ustar25, shelt_sf, c1;
+  int oc;  // 1-based cut-off index; 0-based level o is prognostic when o < oc
+};
+
+__device__ __forceinline__ WindIn load_wind(const Params& prm, const Ptrs& P, int jj, float ustar) {
+  WindIn w;
+  w.wspd = P.wspd[jj];
+  w.uc = P.uc[jj];
+  w.vc = P.vc[jj];
+  w.ustar25 = 2.5f * ustar;
+  w.shelt_sf = P.shelt[jj] / prm.sin_fac;
+  // (1 - fice) * twopi * rhorat
+  w.c1 = ((1.f - P.fice[jj]) * (2.f * 3.14159274f)) * P.rhorat[jj];
+  w.oc = P.oc[jj];
+  return w;
+}
+
+// Sin at (o, p) given cw = cos(wdir - th(p)) and the level tables.
+__device__ __forceinline__ float sin_bin(const Params& prm, const WindIn& w, float cw, float cth, float sth,
+                                         float logl2z, float cp0, float fkovg, bool tail) {
+  float s = (w.wspd + w.ustar25 * logl2z) * cw - cp0 - w.uc * cth - w.vc * sth;
+  s = (prm.sin_fac * fabsf(s)) * s;
+  if (s > 0.f) s = s * w.shelt_sf;
+  if (s < 0.f) s = s * prm.fieldscale1;
+  if (s < 0.f && cw > 0.f) s = s * prm.fieldscale2;
+  s = (w.c1 * s) * fkovg;
+  if (tail) s = fmaxf(s, 0.f);
+  return s;
+}
+
+// Bounded spin on a device flag is never used; all cross-block ordering is
+// by kernel boundaries on one stream.
+
+}  // namespace umwm

@@ -1,0 +1,330 @@
+// Per-substep forcing and cut-off kernel, the dts/dtr control kernel, and the
+// once-per-output kernels: diag, Stokes drift, sea-ice Hs, the screen line
+// and the spectrum layout transposes.
+#include <algorithm>
+#include <cfloat>
+
+#include "dev_common.cuh"
+#include "kernels.hpp"
+
+namespace umwm {
+
+// forcinginterpolate + the global side effects at the top of sin_d12
+// (umwm_forcing.F90:40-99, umwm_source_functions.F90:21-36): per unrolled
+// point (land included) interpolate the 2-d forcing levels in sumt/dtg,
+// clamp wspd, rhorat; per wet point the cut-off index oc and the
+// sheltering coefficient (umwm_source_functions.F90:52).
+__global__ void k_prep(const Params prm, const Ptrs P, int compute_rot) {
+  const float sumt = P.ctl->sumt, dtg = prm.dtg;
+  const float a = 1.f - sumt / dtg;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < prm.NM; i += gridDim.x * blockDim.x) {
+    const int q = (P.mi[i] - 1) + (P.ni[i] - 1) * prm.mm;
+    if (prm.winds) {
+      float uw = P.uwb[q] * a + P.uwf[q] * sumt / dtg;
+      float vw = P.vwb[q] * a + P.vwf[q] * sumt / dtg;
+      P.wspd[i] = sqrtf(uw * uw + vw * vw);
+      P.wdir[i] = atan2f(vw, uw);
+    }
+    if (prm.seaice) P.fice[i] = P.ficeb[q] * a + P.ficef[q] * sumt / dtg;
+    if (prm.currents) {
+      P.uc[i] = P.ucb[q] * a + P.ucf[q] * sumt / dtg;
+      P.vc[i] = P.vcb[q] * a + P.vcf[q] * sumt / dtg;
+    }
+    if (prm.air_density) P.rhoa[i] = P.rhoab[q] * a + P.rhoaf[q] * sumt / dtg;
+    if (prm.water_density) P.rhow[i] = P.rhowb[q] * a + P.rhowf[q] * sumt / dtg;
+    P.rhorat[i] = P.rhoa[i] / P.rhow[i];
+    const float ws = fmaxf(P.wspd[i], 1e-2f);
+    P.wspd[i] = ws;
+    if ((prm.isglobal || i < prm.N) && (P.uc[i] != 0.f || P.vc[i] != 0.f)) P.ctl->anycurrent = 1;
+    if (i < prm.N) {
+      float fc = 0.53f * prm.g / ws;
+      if (fc > prm.fprog) fc = prm.fprog;
+      P.fcutoff[i] = fc;
+      int oc = 1;
+      for (int o = prm.O - 2; o >= 1; --o) {
+        oc = o;
+        if (fc > prm.f[o - 1]) break;
+      }
+      P.oc[i] = oc;
+      if (compute_rot) P.oc_rot[i] = oc;
+      P.shelt[i] = shelter_coare35(ws);
+    }
+  }
+}
+
+// source(): dts = min(min_i physics_time_step, dtamin, dtg - sumt), the
+// first-step rule and sumt update (umwm_physics.F90:41-58); refraction's
+// dtr (umwm_advection.F90:145-158).  One thread.
+__global__ void k_dts(const Params prm, const Ptrs P, int compute_rot, int first) {
+  Ctl& c = *P.ctl;
+  float mn = dec_ord_d(c.minphys_enc);
+  float dts = fminf(fminf(mn, prm.dtamin), prm.dtg - c.sumt);
+  if (!prm.restart && first) dts = 0.f;
+  c.dts = dts;
+  c.dta = dts;
+  c.sumt = c.sumt + dts;
+  if (compute_rot) {
+    float mx = dec_ord_d(c.maxrot_enc);
+    c.dtr_temp = (mx <= FLT_MIN) ? dts : prm.dth / mx;
+  }
+  c.dtr = fminf(c.dtr_temp, dts);
+  c.zerocurrents = c.anycurrent ? 0 : 1;
+  c.anycurrent = 0;
+  c.minphys_enc = enc_ord_d(__int_as_float(0x7f800000));
+  c.maxrot_enc = enc_ord_d(0.f);
+  c.done = (c.sumt < prm.dtg) ? 0 : 1;
+  c.first = first;
+}
+
+// s_ice: significant wave height where fice > fice_lth and the attenuation
+// factor C1*Hs (Hs < 3 m) or C1*3 (umwm_source_functions.F90:108-153).
+__global__ void k_sice(const Params prm, const Ptrs P) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= prm.N) return;
+  float sv = 0.f;
+  if (P.fice[j] > prm.fice_lth) {
+    float h = 0.f;
+    for (int p = 0; p < prm.P; ++p)
+      for (int o = 0; o < prm.O; ++o)
+        h += P.E[((size_t)o * prm.P + p) * prm.ldN + j] * P.TAB[((size_t)o * T_COUNT + T_KDK) * prm.ldN + j];
+    h = 4.f * sqrtf(h * prm.dth);
+    const float C1 = -5.35e-6f;
+    sv = (h < 3.f) ? C1 * h : C1 * 3.f;
+  }
+  P.sice_v[j] = sv;
+}
+
+// diag, umwm_physics.F90:89-205 (one thread per wet point, reference loop order)
+__global__ void k_diag(const Params prm, const Ptrs P) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= prm.N) return;
+  const int O = prm.O, NP = prm.P, ldN = prm.ldN, oc = P.oc[j];
+  const float* E = P.E;
+  auto tab = [&](int t, int o) { return P.TAB[((size_t)o * T_COUNT + t) * ldN + j]; };
+  float m0 = 0.f, m2 = 0.f, m2k = 0.f, mx = 0.f, my = 0.f, cxx = 0.f, cxy = 0.f, cyy = 0.f, xc = 0.f, yc = 0.f;
+  float best = -1.f;
+  int op = 0, pp = 0;
+  for (int p = 0; p < NP; ++p) {
+    float mag = 0.f;
+    const float cth = prm.cth[p], sth = prm.sth[p];
+    for (int o = 0; o < O; ++o) {
+      const float e = E[((size_t)o * NP + p) * ldN + j];
+      const float kdk = tab(T_KDK, o);
+      const float ek = e * kdk;
+      m0 += ek;
+      m2 += (prm.f[o] * prm.f[o]) * e * kdk;
+      m2k += e * tab(T_K3DK, o);
+      mag += ek;
+      if (ek > best) { best = ek; op = o; pp = p; }
+      if (o < oc) {
+        const float ekc = ek / tab(T_CP0, o);
+        const float cg = tab(T_CG0, o);
+        mx += ekc * cth; my += ekc * sth;
+        cxx += cg * ekc * (cth * cth); cxy += cg * ekc * cth * sth; cyy += cg * ekc * (sth * sth);
+      }
+    }
+    xc += mag * cth; yc += mag * sth;
+  }
+  const float rw = P.rhow[j] * prm.dthg;
+  P.mwp[j] = sqrtf(m0 / (m2 + FLT_MIN));
+  P.momx[j] = mx * rw; P.momy[j] = my * rw;
+  P.cgmxx[j] = cxx * rw; P.cgmxy[j] = cxy * rw; P.cgmyy[j] = cyy * rw;
+  P.ht[j] = 4.f * sqrtf(m0 * prm.dth);
+  P.mwd[j] = atan2f(yc, xc);
+  P.mss[j] = m2k * prm.dth;
+  P.mwl[j] = 2.f * 3.14159274f * sqrtf(m0 / (m2k + FLT_MIN));
+  P.dwd[j] = prm.th[pp];
+  P.dwl[j] = 2.f * 3.14159274f / tab(T_K, op);
+  P.dwp[j] = 1.f / prm.f[op];
+  const float c0 = tab(T_CP0, op), g0 = tab(T_CG0, op);
+  P.dcp0[j] = c0; P.dcg0[j] = g0;
+  const float uc = P.uc[j], vc = P.vc[j];
+  P.dcp[j] = c0 + uc * prm.cth[pp] + vc * prm.sth[pp];
+  P.dcg[j] = g0 + uc * prm.cth[pp] + vc * prm.sth[pp];
+}
+
+// stokes_drift, umwm_stokes.F90:55-128: util recomputed from k, d and cg0
+// instead of stored (it would be om*im*lm floats).
+__global__ void k_stokes(const Params prm, const Ptrs P) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= prm.N) return;
+  const int O = prm.O, NP = prm.P, ldN = prm.ldN;
+  float X[MAX_OM], Y[MAX_OM];
+  for (int o = 0; o < O; ++o) {
+    float x = 0.f, y = 0.f;
+    for (int p = 0; p < NP; ++p) {
+      const float e = P.E[((size_t)o * NP + p) * ldN + j];
+      x += e * prm.cth[p];
+      y += e * prm.sth[p];
+    }
+    X[o] = x; Y[o] = y;
+  }
+  const float d = P.d[j];
+  const float twopi = 2.f * 3.14159274f;
+  float um1 = 0.f, usm_prev = 0.f, ds = 0.f, ust_ef = 0.f;
+  bool found = false;
+  for (int l = 0; l < prm.lm; ++l) {
+    const float dep = prm.depth[l];
+    float su = 0.f, sv = 0.f;
+    if (!(fabsf(dep) > d)) {
+      for (int o = 0; o < O; ++o) {
+        const float kk = P.TAB[((size_t)o * T_COUNT + T_K) * ldN + j];
+        const float dwn = prm.dom[o] / fabsf(P.TAB[((size_t)o * T_COUNT + T_CG0) * ldN + j]);
+        const float kd = kk * d;
+        const float arg = 2.f * kk * (dep + d);
+        float u;
+        if (fabsf(arg) > 50.f || kd > 50.f)
+          u = twopi * prm.f[o] * 2.f * (kk * kk) * expf(2.f * kk * dep) * dwn * prm.dth;
+        else {
+          const float sh = sinhf(kd);
+          u = twopi * prm.f[o] * (kk * kk) * coshf(2.f * kk * (dep + d)) / (sh * sh) * dwn * prm.dth;
+        }
+        su += u * X[o];
+        sv += u * Y[o];
+      }
+    }
+    P.us[(size_t)l * ldN + j] = su;
+    P.vs[(size_t)l * ldN + j] = sv;
+    const float um = sqrtf(su * su + sv * sv);
+    if (l == 0) {
+      um1 = um;
+      ust_ef = um1 * prm.eulerinv;
+    } else if (um1 != 0.f && !found && um < ust_ef) {
+      ds = (fabsf(usm_prev - ust_ef) * dep + fabsf(um - ust_ef) * prm.depth[l - 1]) / (usm_prev - um);
+      found = true;
+    }
+    usm_prev = um;
+  }
+  P.ds[j] = -ds;
+}
+
+// Screen line at the print point (umwm_top.F90:143-148, umwm_util.F90:69-124);
+// also clears 'first' after the first substep.
+__global__ void k_screen(const Params prm, const Ptrs P) {
+  __shared__ float s0[256], s2[256];
+  Ctl& c = *P.ctl;
+  const int j = prm.iip;
+  float a = 0.f, b = 0.f;
+  if (j >= 0) {
+    for (int b_ = threadIdx.x; b_ < prm.O * prm.P; b_ += blockDim.x) {
+      const int o = b_ / prm.P;
+      const float ek = P.E[(size_t)b_ * prm.ldN + j] * P.TAB[((size_t)o * T_COUNT + T_KDK) * prm.ldN + j];
+      a += ek;
+      b += (prm.f[o] * prm.f[o]) * ek;
+    }
+  }
+  s0[threadIdx.x] = a;
+  s2[threadIdx.x] = b;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) { s0[threadIdx.x] += s0[threadIdx.x + s]; s2[threadIdx.x] += s2[threadIdx.x + s]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const int r = c.log_count;
+    if (r < P.log_cap && j >= 0) {
+      double* L = P.log + (size_t)r * 8;
+      L[0] = c.sumt / prm.dtg;
+      L[1] = c.dts;
+      L[2] = P.wspd[j];
+      L[3] = P.wdir[j];
+      L[4] = 4.f * sqrtf(s0[0] * prm.dth);
+      L[5] = sqrtf(s0[0] / s2[0]);
+      L[6] = P.cd[j] * 1e3f;
+      L[7] = prm.f[P.oc[j] - 1];
+      c.log_count = r + 1;
+    }
+    c.substep += 1;
+    c.first = 0;
+  }
+}
+
+// Reference order F(om,pm,im) (o fastest) <-> device [o][p][ldN].
+__global__ void k_to_ref(const Params prm, const float* __restrict__ E, float* __restrict__ F) {
+  __shared__ float tile[32][33];
+  const int R = prm.O * prm.P;
+  const int c0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int k = ty; k < 32; k += blockDim.y) {
+    const int c = c0 + k;  // column of F: c = p*O + o
+    if (c < R && j0 + tx < prm.N) {
+      const int o = c % prm.O, p = c / prm.O;
+      tile[k][tx] = E[((size_t)o * prm.P + p) * prm.ldN + j0 + tx];
+    }
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += blockDim.y) {
+    const int jrow = j0 + k, c = c0 + tx;
+    if (jrow < prm.N && c < R) F[(size_t)jrow * R + c] = tile[tx][k];
+  }
+}
+
+__global__ void k_from_ref(const Params prm, const float* __restrict__ F, float* __restrict__ E) {
+  __shared__ float tile[32][33];
+  const int R = prm.O * prm.P;
+  const int c0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int k = ty; k < 32; k += blockDim.y) {
+    const int jrow = j0 + k, c = c0 + tx;
+    if (jrow < prm.N && c < R) tile[k][tx] = F[(size_t)jrow * R + c];
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += blockDim.y) {
+    const int c = c0 + k;
+    if (c < R && j0 + tx < prm.N) {
+      const int o = c % prm.O, p = c / prm.O;
+      E[((size_t)o * prm.P + p) * prm.ldN + j0 + tx] = tile[tx][k];
+    }
+  }
+}
+
+__global__ void k_fill(float* a, size_t n, float v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) a[i] = v;
+}
+
+static int grid_for(long n, int block) {
+  long g = (n + block - 1) / block;
+  if (g > 152L * 32) g = 152L * 32;
+  return (int)(g < 1 ? 1 : g);
+}
+
+cudaError_t launch_prep(const Params& prm, const Ptrs& P, int compute_rot, cudaStream_t st) {
+  k_prep<<<grid_for(prm.NM, 256), 256, 0, st>>>(prm, P, compute_rot);
+  return cudaGetLastError();
+}
+cudaError_t launch_dts(const Params& prm, const Ptrs& P, int compute_rot, int first, cudaStream_t st) {
+  k_dts<<<1, 1, 0, st>>>(prm, P, compute_rot, first);
+  return cudaGetLastError();
+}
+cudaError_t launch_sice(const Params& prm, const Ptrs& P, cudaStream_t st) {
+  k_sice<<<(prm.N + 127) / 128, 128, 0, st>>>(prm, P);
+  return cudaGetLastError();
+}
+cudaError_t launch_diag(const Params& prm, const Ptrs& P, cudaStream_t st) {
+  k_diag<<<(prm.N + 127) / 128, 128, 0, st>>>(prm, P);
+  return cudaGetLastError();
+}
+cudaError_t launch_stokes(const Params& prm, const Ptrs& P, cudaStream_t st) {
+  k_stokes<<<(prm.N + 127) / 128, 128, 0, st>>>(prm, P);
+  return cudaGetLastError();
+}
+cudaError_t launch_screen(const Params& prm, const Ptrs& P, cudaStream_t st) {
+  k_screen<<<1, 256, 0, st>>>(prm, P);
+  return cudaGetLastError();
+}
+cudaError_t launch_to_ref(const Params& prm, const float* E, float* F, cudaStream_t st) {
+  dim3 grid((prm.O * prm.P + 31) / 32, (prm.N + 31) / 32), block(32, 8);
+  k_to_ref<<<grid, block, 0, st>>>(prm, E, F);
+  return cudaGetLastError();
+}
+cudaError_t launch_from_ref(const Params& prm, const float* F, float* E, cudaStream_t st) {
+  dim3 grid((prm.O * prm.P + 31) / 32, (prm.N + 31) / 32), block(32, 8);
+  k_from_ref<<<grid, block, 0, st>>>(prm, F, E);
+  return cudaGetLastError();
+}
+cudaError_t launch_fill(float* a, size_t n, float v, cudaStream_t st) {
+  k_fill<<<grid_for((long)std::min<size_t>(n, 1u << 30), 256), 256, 0, st>>>(a, n, v);
+  return cudaGetLastError();
+}
+
+}  // namespace umwm

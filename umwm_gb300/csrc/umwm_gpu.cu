@@ -1,0 +1,823 @@
+// C ABI of the GB300 UMWM library (include/umwm_gpu.h): the umwm_top entry
+// points, the in-memory stand-ins for the reference's input files, and the
+// device-resident model.  The outer dtg loop and the inner dynamic-dts loop
+// of umwm_run (umwm_top.F90:68-192) are driven from here; every per-substep
+// quantity (dts, sumt, dtr, the rotation max, the screen line) stays in a
+// device control block, and the host reads back one flag per substep to
+// end the inner loop, or none at all when the loop runs as a CUDA graph
+// with a device-side while node.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/umwm_gpu.h"
+#include "host_model.hpp"
+#include "kernels.hpp"
+
+namespace umwm {
+namespace {
+
+std::string g_err;
+Inputs g_inputs;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CU(x)                                                                                   \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess) return fail(UMWM_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+unsigned enc_ord_h(float x) {
+  unsigned u;
+  std::memcpy(&u, &x, 4);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+struct Dev {
+  std::vector<void*> bufs;
+  template <typename T>
+  cudaError_t alloc(T** p, size_t n, bool zero = true) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) return e;
+    bufs.push_back(q);
+    if (zero) e = cudaMemset(q, 0, std::max<size_t>(n, 1) * sizeof(T));
+    *p = (T*)q;
+    return e;
+  }
+  ~Dev() {
+    for (void* q : bufs) cudaFree(q);
+  }
+};
+
+struct Model {
+  HostModel H;
+  bool on_device = false;
+  Params prm{};
+  Ptrs P{};
+  std::unique_ptr<Dev> dev;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int* done_h = nullptr;  // pinned
+  bool first = true, firstdtg = true, readfile = false;
+  long long substeps = 0, max_substeps = -1;
+  bool verbose = false, check_finite = false, use_graph = false;
+  double last_gpu_ms = 0, last_bins = 0;
+  long long launches = 0;
+  size_t screen_printed = 0;
+  // forcing levels on the device (mm*nm each)
+  float *uwb = nullptr, *uwf = nullptr, *vwb = nullptr, *vwf = nullptr, *ucb = nullptr, *ucf = nullptr,
+        *vcb = nullptr, *vcf = nullptr, *rhoab = nullptr, *rhoaf = nullptr, *rhowb = nullptr, *rhowf = nullptr,
+        *ficeb = nullptr, *ficef = nullptr;
+  // writable views of the Ptrs members
+  float *E = nullptr, *ES = nullptr, *EF = nullptr, *TAB = nullptr;
+
+  ~Model() {
+    if (st) cudaStreamDestroy(st);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (done_h) cudaFreeHost(done_h);
+  }
+};
+
+std::unique_ptr<Model> g_model;
+
+int upload(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+  return UMWM_OK;
+}
+
+// per-(o,i) tables in device layout [o][t][ldN]; ghost column N
+std::vector<float> build_tables(const HostModel& H, int ldN) {
+  const int O = H.om, N = H.im;
+  std::vector<float> T((size_t)O * T_COUNT * ldN, 0.f);
+  auto put = [&](int t, const std::vector<float>& src, bool ghost) {
+    for (int o = 1; o <= O; ++o) {
+      float* row = &T[((size_t)(o - 1) * T_COUNT + t) * ldN];
+      for (int i = 1; i <= N; ++i) row[i - 1] = src[H.oi(o, i)];
+      if (ghost) row[N] = src[H.oi(o, 0)];
+    }
+  };
+  put(T_K, H.k, false);
+  put(T_CP0, H.cp0, true);
+  put(T_CG0, H.cg0, true);
+  put(T_LOGL2Z, H.logl2overz, false);
+  put(T_FKOVG, H.fkovg, false);
+  put(T_K4, H.k4, false);
+  put(T_K3DK, H.k3dk, false);
+  put(T_KDK, H.kdk, false);
+  put(T_COTHKD, H.cothkd, false);
+  put(T_SBF, H.sbf, false);
+  put(T_SDV, H.sdv, false);
+  put(T_BF1R, H.bf1r, false);
+  put(T_BF2R, H.bf2r, false);
+  // padding columns past N: keep the ghost values of cp0/cg0 and k=1 so that
+  // lanes beyond N compute finite throw-away values
+  for (int o = 0; o < O; ++o)
+    for (int j = N + 1; j < ldN; ++j) {
+      T[((size_t)o * T_COUNT + T_CP0) * ldN + j] = T[((size_t)o * T_COUNT + T_CP0) * ldN + N];
+      T[((size_t)o * T_COUNT + T_CG0) * ldN + j] = T[((size_t)o * T_COUNT + T_CG0) * ldN + N];
+    }
+  for (int o = 0; o < O; ++o)
+    for (int j = N; j < ldN; ++j) {
+      T[((size_t)o * T_COUNT + T_K) * ldN + j] = 1.f;
+      T[((size_t)o * T_COUNT + T_K4) * ldN + j] = 1.f;
+      T[((size_t)o * T_COUNT + T_KDK) * ldN + j] = 1.f;
+      T[((size_t)o * T_COUNT + T_COTHKD) * ldN + j] = 1.f;
+    }
+  return T;
+}
+
+int set_forcing_constants(Model& M) {
+  // input_nc without file variables: umwm_io.F90:39-83
+  const HostModel& H = M.H;
+  const size_t NM = H.imm;
+  if (!H.winds) {
+    CU(launch_fill(M.P.wspd, NM, H.wspd0, M.st));
+    CU(launch_fill(M.P.wdir, NM, H.wdir0, M.st));
+  }
+  if (!H.currents) {
+    CU(launch_fill(M.P.uc, NM, H.uc0, M.st));
+    CU(launch_fill(M.P.vc, NM, H.vc0, M.st));
+  }
+  if (!H.seaice) CU(launch_fill(M.P.fice, NM, H.fice0, M.st));
+  if (!H.air_density) CU(launch_fill(M.P.rhoa, NM, H.rhoa0, M.st));
+  if (!H.water_density) CU(launch_fill(M.P.rhow, NM, H.rhow0, M.st));
+  return UMWM_OK;
+}
+
+// input_nc(timestr) file variables into the n+1 level, umwm_io.F90:13-93
+int read_forcing(Model& M, const std::string& key, std::vector<float>* uwf_host = nullptr,
+                 std::vector<float>* vwf_host = nullptr) {
+  const HostModel& H = M.H;
+  if (!M.readfile) return UMWM_OK;
+  auto it = g_inputs.forcing.find(key);
+  if (it == g_inputs.forcing.end()) return fail(UMWM_ERR_INPUT, "input_nc: no forcing staged for " + key);
+  const size_t n2 = (size_t)H.mm * H.nm;
+  auto get = [&](const char* var, float* dst, bool zero_land, std::vector<float>* keep) -> int {
+    auto v = it->second.find(var);
+    if (v == it->second.end()) return fail(UMWM_ERR_INPUT, std::string("input_nc: variable ") + var + " missing for " + key);
+    if (v->second.size() != n2) return fail(UMWM_ERR_INPUT, std::string("input_nc: variable ") + var + " has the wrong size");
+    std::vector<float> tmp = v->second;
+    if (zero_land)
+      for (size_t q = 0; q < n2; ++q) if (H.mask[q] == 0) tmp[q] = 0.f;
+    if (keep) *keep = tmp;
+    CU(cudaMemcpyAsync(dst, tmp.data(), n2 * 4, cudaMemcpyHostToDevice, M.st));
+    CU(cudaStreamSynchronize(M.st));
+    return UMWM_OK;
+  };
+  int rc;
+  if (H.winds) {
+    if ((rc = get("uw", M.uwf, false, uwf_host))) return rc;
+    if ((rc = get("vw", M.vwf, false, vwf_host))) return rc;
+  }
+  if (H.currents) {
+    if ((rc = get("uc", M.ucf, true, nullptr))) return rc;
+    if ((rc = get("vc", M.vcf, true, nullptr))) return rc;
+  }
+  if (H.seaice && (rc = get("fice", M.ficef, false, nullptr))) return rc;
+  if (H.air_density && (rc = get("rhoa", M.rhoaf, false, nullptr))) return rc;
+  if (H.water_density && (rc = get("rhow", M.rhowf, false, nullptr))) return rc;
+  return UMWM_OK;
+}
+
+// forcinginput, umwm_forcing.F90:11-37
+int forcing_input(Model& M, const std::string& key) {
+  const HostModel& H = M.H;
+  const size_t b = (size_t)H.mm * H.nm * 4;
+  if (H.winds) { CU(cudaMemcpyAsync(M.uwb, M.uwf, b, cudaMemcpyDeviceToDevice, M.st)); CU(cudaMemcpyAsync(M.vwb, M.vwf, b, cudaMemcpyDeviceToDevice, M.st)); }
+  if (H.currents) { CU(cudaMemcpyAsync(M.ucb, M.ucf, b, cudaMemcpyDeviceToDevice, M.st)); CU(cudaMemcpyAsync(M.vcb, M.vcf, b, cudaMemcpyDeviceToDevice, M.st)); }
+  if (H.air_density) CU(cudaMemcpyAsync(M.rhoab, M.rhoaf, b, cudaMemcpyDeviceToDevice, M.st));
+  if (H.water_density) CU(cudaMemcpyAsync(M.rhowb, M.rhowf, b, cudaMemcpyDeviceToDevice, M.st));
+  if (H.seaice) CU(cudaMemcpyAsync(M.ficeb, M.ficef, b, cudaMemcpyDeviceToDevice, M.st));
+  int rc = read_forcing(M, key);
+  if (rc) return rc;
+  if (M.readfile) return set_forcing_constants(M);
+  return UMWM_OK;
+}
+
+int setup_params(Model& M) {
+  HostModel& H = M.H;
+  if (H.om > MAX_OM) return fail(UMWM_ERR_UNSUPPORTED, "om > 64 is not supported");
+  if (H.pm > MAX_PM || !supported_pm(H.pm))
+    return fail(UMWM_ERR_UNSUPPORTED, "pm must be 4*k with k in {2,3,4,6,8,9,12,16,18}");
+  if (H.lm > MAX_LM) return fail(UMWM_ERR_UNSUPPORTED, "more than 100 Stokes depths");
+  if (H.gustiness > 0) return fail(UMWM_ERR_UNSUPPORTED, "gustiness > 0 (Fortran random_number) is not supported");
+  Params& p = M.prm;
+  p.N = H.im;
+  p.ldN = ((H.im + 1) + 31) / 32 * 32;
+  p.O = H.om; p.P = H.pm; p.NM = H.imm; p.mm = H.mm; p.nm = H.nm; p.lm = H.lm;
+  p.iip = (H.iip >= 1 && H.iip <= H.im) ? H.iip - 1 : -1;
+  p.g = H.g; p.explim = H.explim; p.sin_fac = H.sin_fac; p.fieldscale1 = H.fieldscale1;
+  p.fieldscale2 = H.fieldscale2; p.twopisds_fac = H.twopisds_fac; p.sds_power = H.sds_power;
+  p.inv_sds_power = H.inv_sds_power; p.mss_fac = H.mss_fac; p.snl_fac = H.snl_fac; p.sdt_fac = H.sdt_fac;
+  p.z = H.z; p.nu_air = H.nu_air; p.kappa = H.kappa; p.fprog = H.fprog; p.dth = H.dth; p.dthg = H.dthg;
+  p.oneovdth = H.oneovdth; p.dtamin = H.dtamin; p.dtg = H.dtg; p.fice_lth = H.fice_lth; p.fice_uth = H.fice_uth;
+  p.eulerinv = H.eulerinv; p.rhow0 = H.rhow0;
+  p.winds = H.winds; p.currents = H.currents; p.air_density = H.air_density; p.water_density = H.water_density;
+  p.seaice = H.seaice; p.restart = H.restart; p.curvilinear = H.curvilinear; p.isglobal = H.isglobal;
+  p.ice_possible = H.seaice || (H.fice0 > H.fice_lth);
+  for (int o = 0; o < H.om; ++o) { p.f[o] = H.f[o]; p.dom[o] = H.dom[o]; }
+  for (int q = 0; q < H.pm; ++q) {
+    p.th[q] = H.th[q]; p.cth[q] = H.cth[q]; p.sth[q] = H.sth[q];
+    p.c2th[q] = (float)std::cos(2.0 * (double)H.th[q]);
+    p.s2th[q] = (float)std::sin(2.0 * (double)H.th[q]);
+  }
+  for (int l = 0; l < H.lm; ++l) p.depth[l] = H.depth[l];
+  return UMWM_OK;
+}
+
+int init_device(Model& M) {
+  HostModel& H = M.H;
+  int rc = setup_params(M);
+  if (rc) return rc;
+  const Params& p = M.prm;
+  const int N = p.N, ldN = p.ldN, NM = p.NM;
+  const size_t spec = (size_t)p.O * p.P * ldN;
+  M.dev.reset(new Dev());
+  Dev& D = *M.dev;
+  CU(cudaStreamCreateWithFlags(&M.st, cudaStreamNonBlocking));
+  CU(cudaEventCreate(&M.ev0));
+  CU(cudaEventCreate(&M.ev1));
+  CU(cudaMallocHost(&M.done_h, sizeof(int)));
+  Ptrs& P = M.P;
+  CU(D.alloc(&M.E, spec, false));
+  CU(D.alloc(&M.ES, spec, false));
+  CU(D.alloc(&M.EF, spec, false));
+  P.E = M.E; P.ES = M.ES; P.EF = M.EF;
+  CU(D.alloc(&M.TAB, (size_t)p.O * T_COUNT * ldN, false));
+  P.TAB = M.TAB;
+  {
+    std::vector<float> T = build_tables(H, ldN);
+    CU(cudaMemcpy(M.TAB, T.data(), T.size() * 4, cudaMemcpyHostToDevice));
+  }
+  // wet-point integer arrays
+  auto upload_i = [&](const int** dst, const std::vector<int>& src, bool aliased) -> int {
+    std::vector<int> h(ldN, aliased ? N : 0);
+    for (int i = 1; i <= N; ++i) {
+      int v = src[i];
+      h[i - 1] = aliased ? (v == 0 ? N : v - 1) : v - 1;
+    }
+    int* d = nullptr;
+    CU(D.alloc(&d, ldN));
+    CU(cudaMemcpy(d, h.data(), ldN * 4, cudaMemcpyHostToDevice));
+    *dst = d;
+    return UMWM_OK;
+  };
+  if ((rc = upload_i(&P.ie, H.ie, true)) || (rc = upload_i(&P.iw, H.iw, true)) ||
+      (rc = upload_i(&P.in, H.in, true)) || (rc = upload_i(&P.is, H.is, true)) ||
+      (rc = upload_i(&P.iie, H.iie, false)) || (rc = upload_i(&P.iiw, H.iiw, false)) ||
+      (rc = upload_i(&P.iin, H.iin, false)) || (rc = upload_i(&P.iis, H.iis, false)))
+    return rc;
+  auto upload_f = [&](const float** dst, const std::vector<float>& src) -> int {
+    std::vector<float> h(ldN, 1.f);
+    for (int i = 1; i <= N; ++i) h[i - 1] = src[i];
+    float* d = nullptr;
+    CU(D.alloc(&d, ldN));
+    CU(cudaMemcpy(d, h.data(), ldN * 4, cudaMemcpyHostToDevice));
+    *dst = d;
+    return UMWM_OK;
+  };
+  if ((rc = upload_f(&P.oneovar, H.oneovar)) || (rc = upload_f(&P.oneovdx, H.oneovdx)) ||
+      (rc = upload_f(&P.oneovdy, H.oneovdy)) || (rc = upload_f(&P.dxn, H.dxn)) || (rc = upload_f(&P.dxs, H.dxs)) ||
+      (rc = upload_f(&P.dye, H.dye)) || (rc = upload_f(&P.dyw, H.dyw)) || (rc = upload_f(&P.d, H.d)) ||
+      (rc = upload_f(&P.curv, H.curv_i)))
+    return rc;
+  {
+    std::vector<int> ones(ldN, 1);
+    CU(D.alloc(&P.oc, ldN)); CU(D.alloc(&P.oc_rot, ldN));
+    CU(cudaMemcpy(P.oc, ones.data(), ldN * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(P.oc_rot, ones.data(), ldN * 4, cudaMemcpyHostToDevice));
+  }
+  for (float** q : {&P.ustar, &P.cd, &P.taux, &P.tauy, &P.taux_form, &P.tauy_form, &P.taux_skin, &P.tauy_skin,
+                    &P.taux_diag, &P.tauy_diag, &P.tailatmx, &P.tailatmy, &P.shelt, &P.fcutoff, &P.phys, &P.sice_v,
+                    &P.ds, &P.ht, &P.mwp, &P.mwd, &P.mss, &P.mwl, &P.dwd, &P.dwl, &P.dwp, &P.dcp0, &P.dcp, &P.dcg0,
+                    &P.dcg, &P.momx, &P.momy, &P.cgmxx, &P.cgmxy, &P.cgmyy})
+    CU(D.alloc(q, ldN));
+  for (float** q : {&P.wspd, &P.wdir, &P.uc, &P.vc, &P.rhoa, &P.rhow, &P.rhorat, &P.fice}) CU(D.alloc(q, NM));
+  {
+    std::vector<int> mi(NM), ni(NM);
+    for (int i = 1; i <= NM; ++i) { mi[i - 1] = H.mi[i]; ni[i - 1] = H.ni[i]; }
+    int *dmi, *dni;
+    CU(D.alloc(&dmi, NM)); CU(D.alloc(&dni, NM));
+    CU(cudaMemcpy(dmi, mi.data(), NM * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(dni, ni.data(), NM * 4, cudaMemcpyHostToDevice));
+    P.mi = dmi; P.ni = dni;
+  }
+  const size_t n2 = (size_t)H.mm * H.nm;
+  auto lev = [&](bool on, float** b, float** f) -> int {
+    if (!on) return UMWM_OK;
+    CU(D.alloc(b, n2)); CU(D.alloc(f, n2));
+    return UMWM_OK;
+  };
+  if ((rc = lev(H.winds, &M.uwb, &M.uwf)) || (rc = lev(H.winds, &M.vwb, &M.vwf)) ||
+      (rc = lev(H.currents, &M.ucb, &M.ucf)) || (rc = lev(H.currents, &M.vcb, &M.vcf)) ||
+      (rc = lev(H.air_density, &M.rhoab, &M.rhoaf)) || (rc = lev(H.water_density, &M.rhowb, &M.rhowf)) ||
+      (rc = lev(H.seaice, &M.ficeb, &M.ficef)))
+    return rc;
+  P.uwb = M.uwb; P.uwf = M.uwf; P.vwb = M.vwb; P.vwf = M.vwf; P.ucb = M.ucb; P.ucf = M.ucf; P.vcb = M.vcb;
+  P.vcf = M.vcf; P.rhoab = M.rhoab; P.rhoaf = M.rhoaf; P.rhowb = M.rhowb; P.rhowf = M.rhowf; P.ficeb = M.ficeb;
+  P.ficef = M.ficef;
+  CU(D.alloc(&P.us, (size_t)std::max(1, H.lm) * ldN));
+  CU(D.alloc(&P.vs, (size_t)std::max(1, H.lm) * ldN));
+  CU(D.alloc(&P.ctl, 1));
+  P.log_cap = 1 << 20;
+  CU(D.alloc(&P.log, (size_t)P.log_cap * 8));
+
+  // e = tiny(e), umwm_init.F90:1182 (spectrum and the ghost column of E*)
+  const float tiny = std::numeric_limits<float>::min();
+  CU(launch_fill(M.E, spec, tiny, M.st));
+  CU(launch_fill(M.ES, spec, tiny, M.st));
+  CU(launch_fill(M.EF, spec, 0.f, M.st));
+  // control block
+  Ctl c{};
+  c.minphys_enc = enc_ord_h(std::numeric_limits<float>::infinity());
+  c.maxrot_enc = enc_ord_h(0.f);
+  c.first = 1;
+  c.zerocurrents = 1;
+  CU(cudaMemcpy(P.ctl, &c, sizeof c, cudaMemcpyHostToDevice));
+
+  // input_nc(starttimestr), umwm_top.F90:25
+  M.readfile = H.winds || H.currents || H.air_density || H.water_density || H.seaice;
+  std::vector<float> uwf_h, vwf_h;
+  if ((rc = set_forcing_constants(M))) return rc;
+  if ((rc = read_forcing(M, time_key(H.starttimestr.c_str()), &uwf_h, &vwf_h))) return rc;
+  // init: first-guess drag and friction velocity, umwm_init.F90:1350-1365
+  std::vector<float> wspd(N + 1, H.wspd0);
+  if (H.winds)
+    for (int i = 1; i <= N; ++i) {
+      size_t q = H.i2(H.mi[i], H.ni[i]);
+      wspd[i] = std::sqrt(uwf_h[q] * uwf_h[q] + vwf_h[q] * vwf_h[q]);
+    }
+  std::vector<float> ust(ldN, 0.f), cd(ldN, 0.f);
+  for (int i = 1; i <= N; ++i) {
+    float c_ = 1.2e-3f;
+    if (wspd[i] > 11) c_ = (0.49f + 0.065f * wspd[i]) * 1e-3f;
+    cd[i - 1] = c_;
+    ust[i - 1] = std::sqrt(c_) * wspd[i];
+  }
+  CU(cudaMemcpy(P.ustar, ust.data(), ldN * 4, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(P.cd, cd.data(), ldN * 4, cudaMemcpyHostToDevice));
+  if (H.seaice) {
+    // init copies ficef into fice, umwm_init.F90:1351
+    std::vector<float> fi(NM, 0.f);
+    auto it = g_inputs.forcing.find(time_key(H.starttimestr.c_str()));
+    const std::vector<float>& src = it->second.at("fice");
+    for (int i = 1; i <= NM; ++i) fi[i - 1] = src[H.i2(H.mi[i], H.ni[i])];
+    CU(cudaMemcpy(P.fice, fi.data(), NM * 4, cudaMemcpyHostToDevice));
+  }
+  // stokes_drift('init'), umwm_top.F90:27
+  if (H.lm > 0) CU(launch_stokes(M.prm, P, M.st));
+  CU(cudaStreamSynchronize(M.st));
+  M.first = true;
+  M.firstdtg = !H.restart;
+  M.on_device = true;
+  return UMWM_OK;
+}
+
+int restart_read(Model& M, const std::string& key) {  // umwm_restart.F90:19-56
+  auto it = g_inputs.restarts.find(key);
+  if (it == g_inputs.restarts.end()) return fail(UMWM_ERR_INPUT, "restart_read: no restart staged for " + key);
+  const size_t nF = (size_t)M.prm.O * M.prm.P * M.prm.N;
+  if (it->second.first.size() != nF || it->second.second.size() != (size_t)M.prm.N)
+    return fail(UMWM_ERR_INPUT, "restart_read: restart arrays have the wrong size");
+  return umwm_gpu_set_state(it->second.first.data(), it->second.second.data());
+}
+
+int check_ctl(Model& M) {
+  Ctl c;
+  CU(cudaMemcpy(&c, M.P.ctl, sizeof c, cudaMemcpyDeviceToHost));
+  if (c.err) return fail(UMWM_ERR_TIMEOUT, "a device-side wait gave up");
+  return UMWM_OK;
+}
+
+int substep(Model& M) {
+  const int compute_rot = (M.H.currents || M.first) ? 1 : 0;
+  const Params& prm = M.prm;
+  const Ptrs& P = M.P;
+  CU(launch_prep(prm, P, compute_rot, M.st));
+  if (prm.ice_possible) CU(launch_sice(prm, P, M.st));
+  CU(launch_source_phys(prm, P, compute_rot, M.st));
+  CU(launch_dts(prm, P, compute_rot, M.first ? 1 : 0, M.st));
+  CU(launch_source_integ(prm, P, M.st));
+  CU(launch_advect(prm, P, M.st));
+  M.launches += 6 + (prm.ice_possible ? 1 : 0);
+  if (M.first) {
+    CU(launch_diag(prm, P, M.st));
+    M.launches++;
+    M.first = false;
+  }
+  CU(launch_screen(prm, P, M.st));
+  M.launches++;
+  M.substeps++;
+  return UMWM_OK;
+}
+
+void print_screen(Model& M) {
+  int cnt = 0;
+  if (cudaMemcpy(&cnt, &M.P.ctl->log_count, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return;
+  if ((size_t)cnt <= M.screen_printed) return;
+  std::vector<double> rows((size_t)(cnt - M.screen_printed) * 8);
+  cudaMemcpy(rows.data(), M.P.log + M.screen_printed * 8, rows.size() * 8, cudaMemcpyDeviceToHost);
+  for (size_t r = 0; r < rows.size() / 8; ++r) {
+    const double* L = &rows[r * 8];
+    std::printf("  %4.2f  %8.3f %9.6f %9.6f %9.6f %9.6f %9.6f %9.6f\n", L[0], L[1], L[2], L[3], L[4], L[5], L[6], L[7]);
+  }
+  M.screen_printed = cnt;
+  std::fflush(stdout);
+}
+
+int run_impl(Model& M, const std::string& start, const std::string& stop) {
+  int64_t t0, t1;
+  if (!time_from_string(start, t0) || !time_from_string(stop, t1))
+    return fail(UMWM_ERR_ARG, "umwm_run: times must be 'YYYY-MM-DD hh:mm:ss'");
+  int rc;
+  if (M.first && M.H.restart)
+    if ((rc = restart_read(M, time_key(start.c_str())))) return rc;
+  const long long sub0 = M.substeps;
+  CU(cudaEventRecord(M.ev0, M.st));
+  int64_t now = t0;
+  while (now < t1) {
+    now += std::llround((double)M.H.dtg);
+    const std::string cur = time_to_string(now, '_');
+    if (M.verbose) std::printf("umwm: solver: integrating to time: %s\n", cur.c_str());
+    if ((rc = forcing_input(M, cur))) return rc;
+    CU(cudaMemsetAsync(&M.P.ctl->sumt, 0, sizeof(float), M.st));
+    for (long long inner = 0;; ++inner) {
+      if (inner > 10000000LL) return fail(UMWM_ERR_TIMEOUT, "umwm_run: more than 1e7 substeps in one dtg (dts stuck at 0?)");
+      if (M.max_substeps >= 0 && M.substeps >= M.max_substeps) {
+        CU(cudaEventRecord(M.ev1, M.st));
+        CU(cudaEventSynchronize(M.ev1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, M.ev0, M.ev1);
+        M.last_gpu_ms = ms;
+        M.last_bins = (double)(M.substeps - sub0) * M.prm.N * M.prm.O * M.prm.P;
+        return check_ctl(M);
+      }
+      if ((rc = substep(M))) return rc;
+      CU(cudaMemcpyAsync(M.done_h, &M.P.ctl->done, sizeof(int), cudaMemcpyDeviceToHost, M.st));
+      CU(cudaStreamSynchronize(M.st));
+      if (*M.done_h) break;
+    }
+    M.firstdtg = false;
+    if (M.H.stokes && M.prm.lm > 0) { CU(launch_stokes(M.prm, M.P, M.st)); M.launches++; }
+    CU(launch_diag(M.prm, M.P, M.st));
+    M.launches++;
+    if (M.verbose) print_screen(M);
+  }
+  CU(cudaEventRecord(M.ev1, M.st));
+  CU(cudaEventSynchronize(M.ev1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, M.ev0, M.ev1);
+  M.last_gpu_ms = ms;
+  M.last_bins = (double)(M.substeps - sub0) * M.prm.N * M.prm.O * M.prm.P;
+  return check_ctl(M);
+}
+
+int init_common(const std::string& text, bool device) {
+  g_model.reset();
+  std::unique_ptr<Model> M(new Model());
+  if (!M->H.read_namelist(text)) return fail(UMWM_ERR_NAMELIST, M->H.err);
+  if (!M->H.build(g_inputs)) return fail(UMWM_ERR_INPUT, M->H.err);
+  if (device) {
+    int rc = init_device(*M);
+    if (rc) return rc;
+  }
+  g_model = std::move(M);
+  g_err.clear();
+  return UMWM_OK;
+}
+
+Model* need_model(bool device) {
+  if (!g_model) { fail(UMWM_ERR_STATE, "the model is not initialized"); return nullptr; }
+  if (device && !g_model->on_device) { fail(UMWM_ERR_STATE, "the model has no device state (setup_host only)"); return nullptr; }
+  return g_model.get();
+}
+
+}  // namespace
+}  // namespace umwm
+
+using namespace umwm;
+
+extern "C" {
+
+int umwm_gpu_put_gridtopo(const char* var, const float* field, int mm, int nm) {
+  if (!var || !field || mm < 1 || nm < 1) return fail(UMWM_ERR_ARG, "put_gridtopo: bad arguments");
+  std::string v(var);
+  if (v != "lon" && v != "lat" && v != "z") return fail(UMWM_ERR_ARG, "put_gridtopo: variable must be lon, lat or z");
+  g_inputs.gridtopo[v].assign(field, field + (size_t)mm * nm);
+  return UMWM_OK;
+}
+
+int umwm_gpu_put_exclude(const int* mn, int npairs) {
+  if (npairs < 0 || (npairs > 0 && !mn)) return fail(UMWM_ERR_ARG, "put_exclude: bad arguments");
+  g_inputs.exclude.clear();
+  for (int q = 0; q < npairs; ++q) g_inputs.exclude.push_back({mn[2 * q], mn[2 * q + 1]});
+  return UMWM_OK;
+}
+
+int umwm_gpu_put_forcing(const char* time19, const char* var, const float* field, int mm, int nm) {
+  if (!time19 || !var || !field || mm < 1 || nm < 1) return fail(UMWM_ERR_ARG, "put_forcing: bad arguments");
+  std::string v(var);
+  static const char* ok[] = {"uw", "vw", "uc", "vc", "rhoa", "rhow", "fice"};
+  if (std::find_if(std::begin(ok), std::end(ok), [&](const char* s) { return v == s; }) == std::end(ok))
+    return fail(UMWM_ERR_ARG, "put_forcing: unknown variable " + v);
+  int64_t t;
+  if (!time_from_string(time19, t)) return fail(UMWM_ERR_ARG, "put_forcing: bad time string");
+  g_inputs.forcing[time_key(time19)][v].assign(field, field + (size_t)mm * nm);
+  return UMWM_OK;
+}
+
+int umwm_gpu_put_restart(const char* time19, const float* F, long nF, const float* ust, long nust) {
+  if (!time19 || !F || !ust || nF < 0 || nust < 0) return fail(UMWM_ERR_ARG, "put_restart: bad arguments");
+  g_inputs.restarts[time_key(time19)] = {std::vector<float>(F, F + nF), std::vector<float>(ust, ust + nust)};
+  return UMWM_OK;
+}
+
+int umwm_gpu_clear_inputs(void) {
+  g_inputs = Inputs();
+  return UMWM_OK;
+}
+
+int umwm_gpu_initialize_text(const char* text) {
+  if (!text) return fail(UMWM_ERR_ARG, "initialize: null namelist");
+  return init_common(text, true);
+}
+
+int umwm_gpu_initialize(const char* path) {
+  std::string p = path ? path : "namelists/main.nml";
+  std::ifstream f(p);
+  if (!f) return fail(UMWM_ERR_NAMELIST, "cannot open namelist " + p);
+  std::stringstream ss;
+  ss << f.rdbuf();
+  return init_common(ss.str(), true);
+}
+
+int umwm_gpu_setup_host(const char* text) {
+  if (!text) return fail(UMWM_ERR_ARG, "setup_host: null namelist");
+  return init_common(text, false);
+}
+
+int umwm_gpu_run(const char* start, const char* stop) {
+  Model* M = need_model(true);
+  if (!M) return UMWM_ERR_STATE;
+  if (!start || !stop) return fail(UMWM_ERR_ARG, "run: null time");
+  return run_impl(*M, start, stop);
+}
+
+int umwm_gpu_finalize(void) {
+  g_model.reset();
+  return UMWM_OK;
+}
+
+int umwm_gpu_get_dims(int* dims) {
+  Model* M = need_model(false);
+  if (!M) return UMWM_ERR_STATE;
+  if (!dims) return fail(UMWM_ERR_ARG, "get_dims: null");
+  const HostModel& H = M->H;
+  int v[8] = {H.mm, H.nm, H.om, H.pm, H.im, H.imm, H.lm, (int)M->substeps};
+  std::memcpy(dims, v, sizeof v);
+  return UMWM_OK;
+}
+
+int umwm_gpu_set_state(const float* F, const float* ust) {
+  Model* M = need_model(true);
+  if (!M) return UMWM_ERR_STATE;
+  const Params& p = M->prm;
+  if (F) {
+    const size_t n = (size_t)p.O * p.P * p.N;
+    float* tmp = nullptr;
+    CU(cudaMalloc(&tmp, n * 4));
+    cudaError_t e = cudaMemcpy(tmp, F, n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_from_ref(p, tmp, M->E, M->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(M->st);
+    cudaFree(tmp);
+    CU(e);
+  }
+  if (ust) CU(cudaMemcpy(M->P.ustar, ust, (size_t)p.N * 4, cudaMemcpyHostToDevice));
+  return UMWM_OK;
+}
+
+int umwm_gpu_get_state(float* F, float* ust) {
+  Model* M = need_model(true);
+  if (!M) return UMWM_ERR_STATE;
+  const Params& p = M->prm;
+  CU(cudaStreamSynchronize(M->st));
+  if (F) {
+    const size_t n = (size_t)p.O * p.P * p.N;
+    float* tmp = nullptr;
+    CU(cudaMalloc(&tmp, n * 4));
+    cudaError_t e = launch_to_ref(p, M->E, tmp, M->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(M->st);
+    if (e == cudaSuccess) e = cudaMemcpy(F, tmp, n * 4, cudaMemcpyDeviceToHost);
+    cudaFree(tmp);
+    CU(e);
+  }
+  if (ust) CU(cudaMemcpy(ust, M->P.ustar, (size_t)p.N * 4, cudaMemcpyDeviceToHost));
+  return UMWM_OK;
+}
+
+int umwm_gpu_get_field(const char* name, float* out, long n) {
+  Model* M = need_model(false);
+  if (!M) return UMWM_ERR_STATE;
+  if (!name || !out) return fail(UMWM_ERR_ARG, "get_field: null argument");
+  const HostModel& H = M->H;
+  const std::string s(name);
+  const int N = H.im, NM = H.imm, O = H.om;
+  auto need = [&](long k) { return n >= k ? UMWM_OK : fail(UMWM_ERR_ARG, "get_field: buffer too small for " + s); };
+  // host-side setup fields
+  auto wet_host = [&](const std::vector<float>& v) {
+    if (need(N)) return UMWM_ERR_ARG;
+    for (int i = 1; i <= N; ++i) out[i - 1] = v[i];
+    return UMWM_OK;
+  };
+  auto imm_host = [&](const std::vector<float>& v) {
+    if (need(NM)) return UMWM_ERR_ARG;
+    for (int i = 1; i <= NM; ++i) out[i - 1] = v[i];
+    return UMWM_OK;
+  };
+  auto scalar = [&](float v) {
+    if (need(1)) return UMWM_ERR_ARG;
+    out[0] = v;
+    return UMWM_OK;
+  };
+  if (s == "ar") return wet_host(H.ar);
+  if (s == "oneovar") return wet_host(H.oneovar);
+  if (s == "oneovdx") return wet_host(H.oneovdx);
+  if (s == "oneovdy") return wet_host(H.oneovdy);
+  if (s == "dxn") return wet_host(H.dxn);
+  if (s == "dxs") return wet_host(H.dxs);
+  if (s == "dye") return wet_host(H.dye);
+  if (s == "dyw") return wet_host(H.dyw);
+  if (s == "d") return imm_host(H.d);
+  if (s == "dx") return imm_host(H.dx);
+  if (s == "dy") return imm_host(H.dy);
+  if (s == "f" || s == "th" || s == "depth") {
+    const std::vector<float>& v = s == "f" ? H.f : (s == "th" ? H.th : H.depth);
+    if (need((long)v.size())) return UMWM_ERR_ARG;
+    std::copy(v.begin(), v.end(), out);
+    return UMWM_OK;
+  }
+  if (s == "dtamin") return scalar(H.dtamin);
+  if (s == "cgmax") return scalar(H.cgmax);
+  if (s == "dth") return scalar(H.dth);
+  if (s == "d_2d" || s == "dx_2d" || s == "dy_2d" || s == "curv") {
+    const std::vector<float>& v = s == "d_2d" ? H.d_2d : s == "dx_2d" ? H.dx_2d : s == "dy_2d" ? H.dy_2d : H.curv;
+    if (need((long)v.size())) return UMWM_ERR_ARG;
+    std::copy(v.begin(), v.end(), out);
+    return UMWM_OK;
+  }
+  // tables (om, im) with o fastest; cp0/cg0 (om, 0:im)
+  static const std::pair<const char*, int> tabs[] = {
+      {"k", T_K}, {"cp0", T_CP0}, {"cg0", T_CG0}, {"logl2overz", T_LOGL2Z}, {"fkovg", T_FKOVG}, {"k4", T_K4},
+      {"k3dk", T_K3DK}, {"kdk", T_KDK}, {"cothkd", T_COTHKD}, {"sbf", T_SBF}, {"sdv", T_SDV},
+      {"bf1_renorm", T_BF1R}, {"bf2_renorm", T_BF2R}};
+  for (auto& t : tabs)
+    if (s == t.first) {
+      const bool ghost = (t.second == T_CP0 || t.second == T_CG0);
+      const std::vector<float>& src = t.second == T_K ? H.k : t.second == T_CP0 ? H.cp0 : t.second == T_CG0 ? H.cg0
+          : t.second == T_LOGL2Z ? H.logl2overz : t.second == T_FKOVG ? H.fkovg : t.second == T_K4 ? H.k4
+          : t.second == T_K3DK ? H.k3dk : t.second == T_KDK ? H.kdk : t.second == T_COTHKD ? H.cothkd
+          : t.second == T_SBF ? H.sbf : t.second == T_SDV ? H.sdv : t.second == T_BF1R ? H.bf1r : H.bf2r;
+      const int lo = ghost ? 0 : 1;
+      if (need((long)O * (N - lo + 1))) return UMWM_ERR_ARG;
+      for (int i = lo; i <= N; ++i)
+        for (int o = 1; o <= O; ++o) out[(size_t)(i - lo) * O + (o - 1)] = src[H.oi(o, i)];
+      return UMWM_OK;
+    }
+  if (!M->on_device) return fail(UMWM_ERR_STATE, "get_field: " + s + " needs the device model");
+  const Ptrs& P = M->P;
+  CU(cudaStreamSynchronize(M->st));
+  static const char* wetnames[] = {"ustar", "cd", "taux", "tauy", "taux_form", "tauy_form", "taux_skin",
+                                   "tauy_skin", "taux_diag", "tauy_diag", "tailatmx", "tailatmy", "shelt",
+                                   "fcutoff", "physics_time_step", "ds", "ht", "mwp", "mwd", "mss", "mwl", "dwd",
+                                   "dwl", "dwp", "dcp0", "dcp", "dcg0", "dcg", "momx", "momy", "cgmxx", "cgmxy",
+                                   "cgmyy"};
+  float* const wetptrs[] = {P.ustar, P.cd, P.taux, P.tauy, P.taux_form, P.tauy_form, P.taux_skin, P.tauy_skin,
+                            P.taux_diag, P.tauy_diag, P.tailatmx, P.tailatmy, P.shelt, P.fcutoff, P.phys, P.ds,
+                            P.ht, P.mwp, P.mwd, P.mss, P.mwl, P.dwd, P.dwl, P.dwp, P.dcp0, P.dcp, P.dcg0, P.dcg,
+                            P.momx, P.momy, P.cgmxx, P.cgmxy, P.cgmyy};
+  for (size_t q = 0; q < sizeof(wetnames) / sizeof(wetnames[0]); ++q)
+    if (s == wetnames[q]) {
+      if (need(N)) return UMWM_ERR_ARG;
+      CU(cudaMemcpy(out, wetptrs[q], (size_t)N * 4, cudaMemcpyDeviceToHost));
+      return UMWM_OK;
+    }
+  static const char* allnames[] = {"wspd", "wdir", "uc", "vc", "rhoa", "rhow", "rhorat", "fice"};
+  float* const allptrs[] = {P.wspd, P.wdir, P.uc, P.vc, P.rhoa, P.rhow, P.rhorat, P.fice};
+  for (size_t q = 0; q < 8; ++q)
+    if (s == allnames[q]) {
+      if (need(NM)) return UMWM_ERR_ARG;
+      CU(cudaMemcpy(out, allptrs[q], (size_t)NM * 4, cudaMemcpyDeviceToHost));
+      return UMWM_OK;
+    }
+  if (s == "us" || s == "vs") {
+    if (need((long)H.lm * N)) return UMWM_ERR_ARG;
+    const float* src = s == "us" ? P.us : P.vs;
+    for (int l = 0; l < H.lm; ++l)
+      CU(cudaMemcpy(out + (size_t)l * N, src + (size_t)l * M->prm.ldN, (size_t)N * 4, cudaMemcpyDeviceToHost));
+    return UMWM_OK;
+  }
+  Ctl c;
+  CU(cudaMemcpy(&c, P.ctl, sizeof c, cudaMemcpyDeviceToHost));
+  if (s == "dts") return scalar(c.dts);
+  if (s == "dta") return scalar(c.dta);
+  if (s == "dtr") return scalar(c.dtr);
+  if (s == "dtr_temp") return scalar(c.dtr_temp);
+  if (s == "sumt") return scalar(c.sumt);
+  return fail(UMWM_ERR_ARG, "get_field: unknown field " + s);
+}
+
+int umwm_gpu_get_field_i(const char* name, int* out, long n) {
+  Model* M = need_model(false);
+  if (!M) return UMWM_ERR_STATE;
+  if (!name || !out) return fail(UMWM_ERR_ARG, "get_field_i: null argument");
+  const HostModel& H = M->H;
+  const std::string s(name);
+  auto vec = [&](const std::vector<int>& v, int lo, int hi) {
+    if (n < hi - lo + 1) return fail(UMWM_ERR_ARG, "get_field_i: buffer too small for " + s);
+    for (int i = lo; i <= hi; ++i) out[i - lo] = v[i];
+    return UMWM_OK;
+  };
+  if (s == "mask" || s == "ii") {
+    const std::vector<int>& v = s == "mask" ? H.mask : H.ii;
+    if (n < (long)v.size()) return fail(UMWM_ERR_ARG, "get_field_i: buffer too small");
+    std::copy(v.begin(), v.end(), out);
+    return UMWM_OK;
+  }
+  if (s == "mi") return vec(H.mi, 1, H.imm);
+  if (s == "ni") return vec(H.ni, 1, H.imm);
+  if (s == "iw") return vec(H.iw, 1, H.imm);
+  if (s == "ie") return vec(H.ie, 1, H.imm);
+  if (s == "is") return vec(H.is, 1, H.imm);
+  if (s == "in") return vec(H.in, 1, H.imm);
+  if (s == "iiw") return vec(H.iiw, 1, H.imm);
+  if (s == "iie") return vec(H.iie, 1, H.imm);
+  if (s == "iis") return vec(H.iis, 1, H.imm);
+  if (s == "iin") return vec(H.iin, 1, H.imm);
+  if (s == "im" || s == "imm" || s == "iip") {
+    if (n < 1) return fail(UMWM_ERR_ARG, "get_field_i: buffer too small");
+    out[0] = s == "im" ? H.im : s == "imm" ? H.imm : H.iip;
+    return UMWM_OK;
+  }
+  if (s == "oc") {
+    if (!M->on_device) return fail(UMWM_ERR_STATE, "get_field_i: oc needs the device model");
+    if (n < H.im) return fail(UMWM_ERR_ARG, "get_field_i: buffer too small");
+    CU(cudaMemcpy(out, M->P.oc, (size_t)H.im * 4, cudaMemcpyDeviceToHost));
+    return UMWM_OK;
+  }
+  return fail(UMWM_ERR_ARG, "get_field_i: unknown field " + s);
+}
+
+int umwm_gpu_get_screen(double* out, long n, long* rows) {
+  Model* M = need_model(true);
+  if (!M) return UMWM_ERR_STATE;
+  int cnt = 0;
+  CU(cudaMemcpy(&cnt, &M->P.ctl->log_count, 4, cudaMemcpyDeviceToHost));
+  if (rows) *rows = cnt;
+  if (out && n > 0) {
+    long k = std::min<long>(n / 8, cnt);
+    CU(cudaMemcpy(out, M->P.log, (size_t)k * 8 * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  return UMWM_OK;
+}
+
+int umwm_gpu_set_option(const char* name, double value) {
+  if (!name) return fail(UMWM_ERR_ARG, "set_option: null name");
+  std::string s(name);
+  Model* M = g_model.get();
+  if (!M) return fail(UMWM_ERR_STATE, "set_option: initialize first");
+  if (s == "verbose") { M->verbose = value != 0; return UMWM_OK; }
+  if (s == "max_substeps") { M->max_substeps = (long long)value; return UMWM_OK; }
+  if (s == "check_finite") { M->check_finite = value != 0; return UMWM_OK; }
+  if (s == "use_graph") { M->use_graph = value != 0; return UMWM_OK; }
+  return fail(UMWM_ERR_ARG, "set_option: unknown option " + s);
+}
+
+double umwm_gpu_get_stat(const char* name) {
+  Model* M = g_model.get();
+  if (!M || !name) return -1.0;
+  std::string s(name);
+  if (s == "substeps") return (double)M->substeps;
+  if (s == "gpu_ms") return M->last_gpu_ms;
+  if (s == "bin_updates") return M->last_bins;
+  if (s == "launches") return (double)M->launches;
+  return -1.0;
+}
+
+const char* umwm_gpu_last_error(void) { return g_err.c_str(); }
+
+}  // extern "C"
