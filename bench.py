@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the UMWM time step on GB300.
+
+Unit: bin-update = one wet spectral bin (o, p, i) advanced by one dynamic
+substep dts; every wet point counts om*pm = 1332 bins.  A bench "step" is one
+substep (sources + integration + propagation + refraction + stress) over the
+whole domain.
+
+Workload: the 1000x1000 random-field domain (dx = 2 km, ~20 % land,
+log-Gaussian depth 10-5000 m, winds 0-25 m/s, currents 0-1 m/s, JONSWAP
+restart), seeded synthetic data built by umwm_gb300.configs.random_field.
+The spectrum (4.3 GB per array) is far larger than L2, so no flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 runs N independent replicas (one per GPU, launched by torchrun); the
+model does not shard across GPUs.  value = bins of all ranks / max rank time.
+--impl reference times the CPU restatement of the reference (oracle/) on the
+host cores on a bounded crop of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "bin-updates/s: plain vs batched/surrogate on 1 GB300 at Hs err ≤2% vs FP64"
+UNIT = "bin-updates/s"
+BINS = 37 * 36
+# algorithmic spectrum bytes per bin-update of each kernel: the two phases
+# forced by the dts global min and the neighbour E* are each one read and one
+# write of the fp32 spectrum (8 B); the dts pre-pass reads it once (4 B).
+ALGO_BYTES = {"phys": 4.0, "integ": 8.0, "advect": 8.0}
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class Dist:
+    """torch.distributed for N > 1 (barrier and max over ranks); no-op for N = 1."""
+
+    def __init__(self, world, local_rank, backend=None):
+        self.world = world
+        self.torch = None
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+
+            self.torch = torch
+            self.dist = dist
+            if backend is None:
+                backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(local_rank)
+            dist.init_process_group(backend)
+            self.dev = torch.device("cuda", local_rank) if backend == "nccl" else torch.device("cpu")
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64, device=self.dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64, device=self.dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+def aggregate(bins_per_rank, seconds_per_rank):
+    """Whole-job throughput: all ranks' bin-updates over the slowest rank's time."""
+    return float(sum(bins_per_rank)) / float(max(seconds_per_rank))
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_per_bin():
+    """DRAM bytes per bin-update of each kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def cpu_baseline(size, steps, threads):
+    """The oracle (fp32 restatement of the reference, OpenMP over wet points)
+    on a size x size crop of the workload's generator."""
+    from oracle import pyoracle
+    from umwm_gb300 import configs
+
+    case = configs.random_field(mm=size, nm=size, hours=3)
+    nt = pyoracle.set_threads(threads)
+    o = pyoracle.Oracle(case.nml, 32)
+    case.stage(o)
+    o.initialize()
+    o.set_option("max_substeps", 1)  # warm-up substep
+    o.run(case.start, case.stop)
+    im = int(o.scalar("im"))
+    o.set_option("max_substeps", 1 + steps)
+    t0 = time.perf_counter()
+    o.run(case.start, case.stop)
+    dt = time.perf_counter() - t0
+    n = int(o.scalar("substeps")) - 1
+    return {"value": n * im * BINS / dt, "unit": UNIT, "cores": nt, "kind": "port",
+            "sample": "random_field %dx%d (%d wet points), %d substeps, fp32 oracle" % (size, size, im, n)}
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    from oracle import pyoracle
+    from umwm_gb300 import configs
+
+    case = configs.random_field(mm=args.ref_size, nm=args.ref_size, hours=3)
+    nt = pyoracle.set_threads(threads)
+    o = pyoracle.Oracle(case.nml, 32)
+    case.stage(o)
+    o.initialize()
+    im = int(o.scalar("im"))
+    o.set_option("max_substeps", args.warmup)
+    o.run(case.start, case.stop)
+    done = int(o.scalar("substeps"))
+    target = done + args.steps
+    t0 = time.perf_counter()
+    while done < target:
+        o.set_option("max_substeps", target)
+        o.run(case.start, case.stop)
+        done = int(o.scalar("substeps"))
+    dt = time.perf_counter() - t0
+    value = args.steps * im * BINS / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "random_field %dx%d crop of the 1000x1000 workload (%d wet points)"
+                                   % (args.ref_size, args.ref_size, im), "wet_points": im, "bins_per_point": BINS},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port",
+                             "sample": "%d substeps of a %dx%d crop, fp32 oracle (CPU restatement of the reference;"
+                                       " the Fortran reference cannot be built: no Fortran compiler or netCDF)"
+                                       % (args.steps, args.ref_size, args.ref_size)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=1000, help="domain is size x size")
+    ap.add_argument("--ref-size", type=int, default=200, help="crop for the CPU legs")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    rank, world, local_rank = rank_info()
+    dist = Dist(world, local_rank)
+    import umwm_gb300 as U
+    from umwm_gb300 import configs
+
+    case = configs.random_field(mm=args.size, nm=args.size, hours=3)
+    U.set_option("device", local_rank)
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=case.nml)
+    N = U.dims()["im"]
+    case.restart = None  # drop the host copy of the 4.3 GB restart spectrum
+    U.clear_inputs()
+    for t, vars_ in case.forcing.items():
+        for var, fld in vars_.items():
+            U.put_forcing(t, var, fld)
+
+    def advance_to(target):
+        while U.dims()["substeps"] < target:
+            U.set_option("max_substeps", target)
+            U.umwm_run(case.start, case.stop)
+
+    advance_to(args.warmup)
+    sub0 = U.dims()["substeps"]
+    U.set_option("kernel_timing", 1)
+    launches0 = U.stat("launches")
+    clocks = Clocks(local_rank)
+    dist.barrier()
+    clocks.start()
+    gpu_ms = 0.0
+    t0 = time.perf_counter()
+    while U.dims()["substeps"] < sub0 + args.steps:
+        U.set_option("max_substeps", sub0 + args.steps)
+        U.umwm_run(case.start, case.stop)
+        gpu_ms += U.stat("gpu_ms")
+    wall = time.perf_counter() - t0
+    dist.barrier()
+    clk = clocks.stop()
+    launches = int(U.stat("launches") - launches0)
+    kms = {k: U.stat("ms:" + k) for k in ("prep", "sice", "phys", "dts", "integ", "advect", "diag", "screen",
+                                          "stokes")}
+    kcnt = {k: U.stat("count:" + k) for k in kms}
+    U.set_option("kernel_timing", 0)
+    nsteps = U.dims()["substeps"] - sub0
+    bins_rank = float(nsteps) * N * BINS
+    t_max = dist.max(gpu_ms / 1e3)
+    bins_all = dist.sum(bins_rank)
+    value = bins_all / t_max
+
+    # end-to-end through the public API: stage one dtg of forcing from host
+    # buffers, run that dtg, read back Hs and ustar
+    e2e = None
+    if not args.no_e2e:
+        U.set_option("max_substeps", -1)
+        f1 = case.forcing[sorted(case.forcing)[1]]
+        s_before = U.dims()["substeps"]
+        dist.barrier()
+        t0 = time.perf_counter()
+        for var, fld in f1.items():
+            U.put_forcing(sorted(case.forcing)[1], var, fld)
+        U.umwm_run(case.start, sorted(case.forcing)[1])
+        hs = U.get_field("ht")
+        us = U.get_field("ustar")
+        te = time.perf_counter() - t0
+        ns = U.dims()["substeps"] - s_before
+        te = dist.max(te)
+        e_bins = dist.sum(float(ns) * N * BINS)
+        h2d = sum(np.asarray(v).nbytes for v in f1.values())
+        d2h = hs.nbytes + us.nbytes + 4 * ns
+        e2e = {"value": e_bins / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d / max(ns, 1)),
+               "d2h_bytes_per_step": int(d2h / max(ns, 1)), "substeps": ns,
+               "note": "one dtg (3600 s) through umwm_gpu_run: forcing staged from host arrays and copied in, "
+                       "Hs and ustar read back"}
+        assert np.isfinite(hs).all()
+
+    peak, peak_kind = peak_hbm()
+    dom = max(("phys", "integ", "advect"), key=lambda k: kms[k])
+    launch_s = kms[dom] / 1e3 / max(kcnt[dom], 1)
+    achieved = ALGO_BYTES[dom] * N * BINS / launch_s / 1e9
+    tr = traffic_per_bin().get(dom)
+    roof = {"bound": "hbm", "kernel": "k_" + dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": peak_kind,
+            "traffic": (tr * N * BINS) if tr is not None else None,
+            "algorithmic_bytes_per_bin": ALGO_BYTES[dom],
+            "step_frac_16B": 16.0 * (bins_rank / (gpu_ms / 1e3)) / 1e9 / peak}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(args.ref_size, args.cpu_steps, os.cpu_count() or 1)
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": nsteps,
+            "warmup": args.warmup, "ms_per_step": t_max * 1e3 / nsteps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "random_field %dx%d dx=2km, plain path (wet points %d, %d bins each); inputs "
+                                   "larger than L2 (spectrum %.1f GB per array)" % (args.size, args.size, N, BINS,
+                                                                                   N * BINS * 4 / 1e9),
+                       "wet_points": N, "bins_per_point": BINS, "replicas": world},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk, "kernel_ms_per_step": {k: kms[k] / max(nsteps, 1) for k in kms if kms[k] > 0},
+            "wall_ms_per_step": wall * 1e3 / nsteps}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    U.umwm_finalize()
+    dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -28,3 +28,12 @@ def rel_err(a, b, floor_frac=1e-6):
     if not m.any():
         return float(np.abs(a - b).max()) if a.size else 0.0
     return float((np.abs(a[m] - b[m]) / np.abs(b[m])).max())
+
+
+def vec_err(ax, ay, bx, by):
+    """Max |a - b| of a 2-vector field relative to the largest |b|."""
+    ax, ay, bx, by = (np.asarray(v, dtype=np.float64) for v in (ax, ay, bx, by))
+    scale = np.hypot(bx, by).max()
+    if scale == 0:
+        return float(max(np.abs(ax).max(), np.abs(ay).max()))
+    return float(max(np.abs(ax - bx).max(), np.abs(ay - by).max()) / scale)

@@ -11,7 +11,7 @@ full run must agree to 2 %.
 import numpy as np
 import pytest
 
-from helpers import rel_err, run_gpu, run_oracle
+from helpers import rel_err, run_gpu, run_oracle, vec_err
 
 pytestmark = pytest.mark.gpu
 
@@ -24,7 +24,11 @@ def U(lib_built):
     return lib_built
 
 
-def _compare_state(U, o, tol_spec, tol_field, fields=("ustar", "cd", "taux", "tauy")):
+VECTORS = [("taux", "tauy"), ("taux_form", "tauy_form"), ("taux_skin", "tauy_skin"), ("tailatmx", "tailatmy"),
+           ("taux_diag", "tauy_diag")]
+
+
+def _compare_state(U, o, tol_spec, tol_field, fields=("ustar", "cd"), vectors=VECTORS[:1]):
     F, ust = U.get_state()
     Fo = o.get("e")
     assert np.isfinite(F).all()
@@ -35,6 +39,9 @@ def _compare_state(U, o, tol_spec, tol_field, fields=("ustar", "cd", "taux", "ta
         b = o.get(name)
         e = rel_err(a, b, 1e-3)
         assert e < tol_field, "%s rel err %.3g" % (name, e)
+    for nx, ny in vectors:
+        e = vec_err(U.get_field(nx), U.get_field(ny), o.get(nx), o.get(ny))
+        assert e < tol_field, "(%s, %s) err %.3g of max |tau|" % (nx, ny, e)
     return err
 
 
@@ -67,8 +74,7 @@ def test_substeps_random_field(U, oracle_mod, nsub):
     case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0)
     run_gpu(U, case, max_substeps=nsub)
     o = run_oracle(oracle_mod, case, 32, max_substeps=nsub)
-    _compare_state(U, o, 1e-3, 1e-3, fields=("ustar", "cd", "taux", "tauy", "taux_form", "tauy_form",
-                                            "taux_skin", "tauy_skin", "tailatmx", "tailatmy"))
+    _compare_state(U, o, 1e-3, 1e-3, vectors=VECTORS)
 
 
 def test_cold_start_reference_namelist(U, oracle_mod):

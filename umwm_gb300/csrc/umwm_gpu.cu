@@ -28,6 +28,11 @@ namespace {
 
 std::string g_err;
 Inputs g_inputs;
+int g_device = -1;  // set_option("device", n) before initialize
+
+// Per-kernel CUDA-event timing on the launching stream (option "kernel_timing").
+enum KName { K_PREP, K_SICE, K_PHYS, K_DTS, K_INTEG, K_ADVECT, K_DIAG, K_SCREEN, K_STOKES, K_NK };
+const char* const KNAMES[K_NK] = {"prep", "sice", "phys", "dts", "integ", "advect", "diag", "screen", "stokes"};
 
 int fail(int code, const std::string& msg) {
   g_err = msg;
@@ -78,6 +83,12 @@ struct Model {
   double last_gpu_ms = 0, last_bins = 0;
   long long launches = 0;
   size_t screen_printed = 0;
+  bool ktime = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> kev;  // pending (kernel, events)
+  std::vector<cudaEvent_t> evpool;
+  size_t evused = 0;
+  double kms[K_NK] = {0};
+  long long kcnt[K_NK] = {0};
   // forcing levels on the device (mm*nm each)
   float *uwb = nullptr, *uwf = nullptr, *vwb = nullptr, *vwf = nullptr, *ucb = nullptr, *ucf = nullptr,
         *vcb = nullptr, *vcf = nullptr, *rhoab = nullptr, *rhoaf = nullptr, *rhowb = nullptr, *rhowf = nullptr,
@@ -86,6 +97,7 @@ struct Model {
   float *E = nullptr, *ES = nullptr, *EF = nullptr, *TAB = nullptr;
 
   ~Model() {
+    for (cudaEvent_t e : evpool) cudaEventDestroy(e);
     if (st) cudaStreamDestroy(st);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
@@ -95,9 +107,38 @@ struct Model {
 
 std::unique_ptr<Model> g_model;
 
-int upload(void* dst, const void* src, size_t bytes, cudaStream_t st) {
-  CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
-  return UMWM_OK;
+cudaEvent_t next_event(Model& M) {
+  if (M.evused == M.evpool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    M.evpool.push_back(e);
+  }
+  return M.evpool[M.evused++];
+}
+
+// Launch wrapper: brackets the launch with events when kernel timing is on.
+template <typename F>
+cudaError_t timed(Model& M, int kname, F&& launch) {
+  if (!M.ktime) return launch();
+  cudaEvent_t a = next_event(M), b = next_event(M);
+  cudaEventRecord(a, M.st);
+  cudaError_t e = launch();
+  cudaEventRecord(b, M.st);
+  M.kev.push_back({kname, {a, b}});
+  return e;
+}
+
+// Collect the timings of completed launches (call after a stream sync).
+void collect_timings(Model& M) {
+  for (auto& k : M.kev) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, k.second.first, k.second.second) == cudaSuccess) {
+      M.kms[k.first] += ms;
+      M.kcnt[k.first] += 1;
+    }
+  }
+  M.kev.clear();
+  M.evused = 0;
 }
 
 // per-(o,i) tables in device layout [o][t][ldN]; ghost column N
@@ -247,6 +288,7 @@ int init_device(Model& M) {
   const Params& p = M.prm;
   const int N = p.N, ldN = p.ldN, NM = p.NM;
   const size_t spec = (size_t)p.O * p.P * ldN;
+  if (g_device >= 0) CU(cudaSetDevice(g_device));
   M.dev.reset(new Dev());
   Dev& D = *M.dev;
   CU(cudaStreamCreateWithFlags(&M.st, cudaStreamNonBlocking));
@@ -408,19 +450,20 @@ int substep(Model& M) {
   const int compute_rot = (M.H.currents || M.first) ? 1 : 0;
   const Params& prm = M.prm;
   const Ptrs& P = M.P;
-  CU(launch_prep(prm, P, compute_rot, M.st));
-  if (prm.ice_possible) CU(launch_sice(prm, P, M.st));
-  CU(launch_source_phys(prm, P, compute_rot, M.st));
-  CU(launch_dts(prm, P, compute_rot, M.first ? 1 : 0, M.st));
-  CU(launch_source_integ(prm, P, M.st));
-  CU(launch_advect(prm, P, M.st));
-  M.launches += 6 + (prm.ice_possible ? 1 : 0);
+  const int first = M.first ? 1 : 0;
+  CU(timed(M, K_PREP, [&] { return launch_prep(prm, P, compute_rot, M.st); }));
+  if (prm.ice_possible) CU(timed(M, K_SICE, [&] { return launch_sice(prm, P, M.st); }));
+  CU(timed(M, K_PHYS, [&] { return launch_source_phys(prm, P, compute_rot, M.st); }));
+  CU(timed(M, K_DTS, [&] { return launch_dts(prm, P, compute_rot, first, M.st); }));
+  CU(timed(M, K_INTEG, [&] { return launch_source_integ(prm, P, M.st); }));
+  CU(timed(M, K_ADVECT, [&] { return launch_advect(prm, P, M.st); }));
+  M.launches += 5 + (prm.ice_possible ? 1 : 0);
   if (M.first) {
-    CU(launch_diag(prm, P, M.st));
+    CU(timed(M, K_DIAG, [&] { return launch_diag(prm, P, M.st); }));
     M.launches++;
     M.first = false;
   }
-  CU(launch_screen(prm, P, M.st));
+  CU(timed(M, K_SCREEN, [&] { return launch_screen(prm, P, M.st); }));
   M.launches++;
   M.substeps++;
   return UMWM_OK;
@@ -465,16 +508,21 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
         cudaEventElapsedTime(&ms, M.ev0, M.ev1);
         M.last_gpu_ms = ms;
         M.last_bins = (double)(M.substeps - sub0) * M.prm.N * M.prm.O * M.prm.P;
+        collect_timings(M);
         return check_ctl(M);
       }
       if ((rc = substep(M))) return rc;
       CU(cudaMemcpyAsync(M.done_h, &M.P.ctl->done, sizeof(int), cudaMemcpyDeviceToHost, M.st));
       CU(cudaStreamSynchronize(M.st));
+      collect_timings(M);
       if (*M.done_h) break;
     }
     M.firstdtg = false;
-    if (M.H.stokes && M.prm.lm > 0) { CU(launch_stokes(M.prm, M.P, M.st)); M.launches++; }
-    CU(launch_diag(M.prm, M.P, M.st));
+    if (M.H.stokes && M.prm.lm > 0) {
+      CU(timed(M, K_STOKES, [&] { return launch_stokes(M.prm, M.P, M.st); }));
+      M.launches++;
+    }
+    CU(timed(M, K_DIAG, [&] { return launch_diag(M.prm, M.P, M.st); }));
     M.launches++;
     if (M.verbose) print_screen(M);
   }
@@ -484,6 +532,7 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
   cudaEventElapsedTime(&ms, M.ev0, M.ev1);
   M.last_gpu_ms = ms;
   M.last_bins = (double)(M.substeps - sub0) * M.prm.N * M.prm.O * M.prm.P;
+  collect_timings(M);
   return check_ctl(M);
 }
 
@@ -798,8 +847,14 @@ int umwm_gpu_get_screen(double* out, long n, long* rows) {
 int umwm_gpu_set_option(const char* name, double value) {
   if (!name) return fail(UMWM_ERR_ARG, "set_option: null name");
   std::string s(name);
+  if (s == "device") { g_device = (int)value; return UMWM_OK; }
   Model* M = g_model.get();
   if (!M) return fail(UMWM_ERR_STATE, "set_option: initialize first");
+  if (s == "kernel_timing") {
+    M->ktime = value != 0;
+    for (int k = 0; k < K_NK; ++k) { M->kms[k] = 0; M->kcnt[k] = 0; }
+    return UMWM_OK;
+  }
   if (s == "verbose") { M->verbose = value != 0; return UMWM_OK; }
   if (s == "max_substeps") { M->max_substeps = (long long)value; return UMWM_OK; }
   if (s == "check_finite") { M->check_finite = value != 0; return UMWM_OK; }
@@ -815,6 +870,10 @@ double umwm_gpu_get_stat(const char* name) {
   if (s == "gpu_ms") return M->last_gpu_ms;
   if (s == "bin_updates") return M->last_bins;
   if (s == "launches") return (double)M->launches;
+  for (int k = 0; k < K_NK; ++k) {
+    if (s == std::string("ms:") + KNAMES[k]) return M->kms[k];
+    if (s == std::string("count:") + KNAMES[k]) return (double)M->kcnt[k];
+  }
   return -1.0;
 }
 
