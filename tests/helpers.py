@@ -37,3 +37,14 @@ def vec_err(ax, ay, bx, by):
     if scale == 0:
         return float(max(np.abs(ax).max(), np.abs(ay).max()))
     return float(max(np.abs(ax - bx).max(), np.abs(ay - by).max()) / scale)
+
+
+def spec_stats(a, b, floor_frac=1e-6):
+    """Relative L2 norm, 99.9th percentile and max of the bin-wise relative
+    error of spectrum a against b (bins of b above floor_frac * max b)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    l2 = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    m = np.abs(b) > floor_frac * np.abs(b).max()
+    r = np.abs(a[m] - b[m]) / np.abs(b[m])
+    return l2, float(np.percentile(r, 99.9)), float(r.max())

@@ -1,21 +1,29 @@
 """GPU parity: the CUDA path through the C ABI against the oracle (CPU
 restatement of the reference) on the same seeded inputs.
 
-Tolerances (fp32 GPU vs fp32 oracle): the GPU rewrites the mean-square-slope
-circulant as an exact rank-3 sum and evaluates pow/exp through the SFU, so
-results differ from the oracle by rounding only; after one substep the
-spectrum must agree to 1e-4 relative on bins above 1e-6 of the maximum, and
-the fields after a few substeps to 1e-3.  Against the fp64 oracle, Hs after a
-full run must agree to 2 %.
+The GPU rewrites the mean-square-slope circulant as an exact rank-3 sum and
+evaluates pow/exp through the SFU, so it differs from the fp32 oracle by
+rounding only.  fp32 rounding itself is amplified where propagation nearly
+empties a bin (the fp32 oracle differs from the fp64 oracle by up to ~1e-2
+relative at such bins after one substep, median 4e-7), so the spectrum
+criteria are:
+  * relative L2 error vs the fp32 oracle <= 1e-5 after one substep
+    (1e-4 after several), 99.9th percentile of the bin-wise relative error
+    <= 1e-3 on bins above 1e-6 of the maximum;
+  * the GPU is no further from the fp64 oracle than the fp32 oracle is:
+    max rel err(GPU, fp64) <= 2 * max rel err(oracle fp32, fp64) + 1e-5.
+Per-point fields (ustar, cd) agree to 1e-3 relative, stress vectors to 1e-3
+of the largest stress.  Against the fp64 oracle, Hs after a full run must
+agree to 2 %.
 """
 import numpy as np
 import pytest
 
-from helpers import rel_err, run_gpu, run_oracle, vec_err
+from helpers import rel_err, run_gpu, run_oracle, spec_stats, vec_err
 
 pytestmark = pytest.mark.gpu
 
-SPEC_TOL_1 = 1e-4
+SPEC_TOL_1 = 1e-5
 FIELD_TOL = 1e-3
 
 
@@ -28,12 +36,19 @@ VECTORS = [("taux", "tauy"), ("taux_form", "tauy_form"), ("taux_skin", "tauy_ski
            ("taux_diag", "tauy_diag")]
 
 
-def _compare_state(U, o, tol_spec, tol_field, fields=("ustar", "cd"), vectors=VECTORS[:1]):
+def _compare_state(U, o, tol_spec, tol_field, fields=("ustar", "cd"), vectors=VECTORS[:1], o64=None):
     F, ust = U.get_state()
     Fo = o.get("e")
     assert np.isfinite(F).all()
-    err = rel_err(F, Fo)
-    assert err < tol_spec, "spectrum rel err %.3g" % err
+    l2, p999, mx = spec_stats(F, Fo)
+    assert l2 < tol_spec, "spectrum relative L2 error %.3g" % l2
+    assert p999 < 1e-3, "spectrum 99.9th percentile rel err %.3g" % p999
+    if o64 is not None:
+        F64 = o64.get("e")
+        g = spec_stats(F, F64)[2]
+        c = spec_stats(Fo, F64)[2]
+        assert g <= 2 * c + 1e-5, "GPU max rel err vs fp64 %.3g > 2 x fp32 oracle's %.3g" % (g, c)
+    err = l2
     for name in fields:
         a = U.get_field(name)
         b = o.get(name)
@@ -51,8 +66,9 @@ def test_one_substep_fetch_limited(U, oracle_mod):
     case = configs.fetch_limited(mm=24, nm=14, hours=1)
     run_gpu(U, case, max_substeps=1)
     o = run_oracle(oracle_mod, case, 32, max_substeps=1)
+    o64 = run_oracle(oracle_mod, case, 64, max_substeps=1)
     assert abs(U.get_field("dts") - o.scalar("dts")) <= 1e-5 * o.scalar("dts")
-    _compare_state(U, o, SPEC_TOL_1, FIELD_TOL)
+    _compare_state(U, o, SPEC_TOL_1, FIELD_TOL, o64=o64)
     assert np.array_equal(U.get_field_i("oc"), o.get("oc").astype(np.int32))
 
 
@@ -62,9 +78,10 @@ def test_one_substep_random_field(U, oracle_mod):
     case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0)
     run_gpu(U, case, max_substeps=1)
     o = run_oracle(oracle_mod, case, 32, max_substeps=1)
+    o64 = run_oracle(oracle_mod, case, 64, max_substeps=1)
     assert abs(U.get_field("dts") - o.scalar("dts")) <= 1e-5 * o.scalar("dts")
     assert abs(U.get_field("dtr") - o.scalar("dtr")) <= 1e-5 * max(o.scalar("dtr"), 1e-30)
-    _compare_state(U, o, SPEC_TOL_1, FIELD_TOL)
+    _compare_state(U, o, SPEC_TOL_1, FIELD_TOL, o64=o64)
 
 
 @pytest.mark.parametrize("nsub", [8])
@@ -74,7 +91,8 @@ def test_substeps_random_field(U, oracle_mod, nsub):
     case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0)
     run_gpu(U, case, max_substeps=nsub)
     o = run_oracle(oracle_mod, case, 32, max_substeps=nsub)
-    _compare_state(U, o, 1e-3, 1e-3, vectors=VECTORS)
+    o64 = run_oracle(oracle_mod, case, 64, max_substeps=nsub)
+    _compare_state(U, o, 1e-4, 1e-3, vectors=VECTORS, o64=o64)
 
 
 def test_cold_start_reference_namelist(U, oracle_mod):
