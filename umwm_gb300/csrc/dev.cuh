@@ -1,11 +1,15 @@
 // Device-side definitions shared by the GB300 UMWM kernels.
 //
-// HBM layout (N wet points, ghost column at index N, row pitch ldN, a
-// multiple of 32 floats so every row starts on a 128-byte boundary):
+// HBM layout.  N wet points plus a ghost point at index N (the reference's
+// aliased land neighbour iistart-1), grouped in NB = ceil((N+1)/32) blocks
+// of 32 consecutive wet points (ldN = 32 NB):
 //   spectrum arrays E, ES (= E* after the source half-step), EF:
-//       [o][p][ldN]  -- the wet index is fastest, so a warp reads 32
-//       consecutive points of one (o,p) bin as one 128-byte line
-//   per-(o,i) tables TAB: [o][table][ldN], tables T_* below
+//       [o][j/32][p][32]: one frequency of one 32-point block is a
+//       contiguous P*128-byte region; within it direction p is a 128-byte
+//       line of 32 consecutive points, so a warp reading one bin for 16 or
+//       32 points is one coalesced access and every direction offset is a
+//       compile-time immediate
+//   per-(o,i) tables TAB: [o][j/32][table][32], tables T_* below
 //   per-point arrays: [ldN]; all-point (land included) arrays: [imm]
 #pragma once
 #include <cstdint>
@@ -35,7 +39,7 @@ enum TableRow {
 };
 
 struct Params {
-  int N, ldN, O, P, NM, mm, nm, lm;
+  int N, ldN, NB, O, P, NM, mm, nm, lm;
   int iip;  // 0-based wet index of the screen point, -1 if none
   float g, explim, sin_fac, fieldscale1, fieldscale2, twopisds_fac, sds_power, inv_sds_power, mss_fac, snl_fac,
       sdt_fac, z, nu_air, kappa, fprog, dth, dthg, oneovdth, dtamin, dtg, fice_lth, fice_uth, eulerinv, rhow0;
@@ -92,5 +96,13 @@ struct Ptrs {
   double* log;  // screen lines, 8 per substep
   int log_cap;
 };
+
+// element offsets in the blocked layouts
+__host__ __device__ inline size_t sidx(const Params& prm, int o, int p, int j) {
+  return ((size_t)(o * prm.NB + (j >> 5)) * prm.P + p) * 32 + (j & 31);
+}
+__host__ __device__ inline size_t tidx(const Params& prm, int o, int t, int j) {
+  return ((size_t)(o * prm.NB + (j >> 5)) * T_COUNT + t) * 32 + (j & 31);
+}
 
 }  // namespace umwm

@@ -1,25 +1,30 @@
 // Propagation, refraction, e = ef and stress('atm') in one pass
 // (umwm_advection.F90:18-180, umwm_top.F90:113-115, umwm_stress.F90:17-264).
 //
-// Same tiling as the source kernels: 32 consecutive wet points per CTA
-// (lane = point), 4 warps over contiguous direction groups.  E* (ES) is read
-// at the point and its four unrolled neighbours; the east/west neighbours
-// sit one wet column away (about nm indices) and are served from L2, which
-// holds the few-MB window of rows that the CTAs in flight are working on.
-// Refraction needs E* at p-1 and p+1; the group's two edge directions are
-// loaded as well.  The rotation rate is recomputed from cp0 and the
-// currents instead of being stored (it depends on no spectral value); when
-// the reference would reuse the rotation of an earlier substep
+// Same thread mapping as the source kernels: a warp owns 16 consecutive wet
+// points, lane = point + 16 * half, half h takes directions h*H .. h*H+H-1
+// with compile-time direction constants and a per-lane sign.
+//
+// Propagation.  cg0 > 0, so for an edge velocity cge = (cg0_i + cg0_ie) c,
+// (cge + |cge|) = 2 (cg0_i + cg0_ie) max(c, 0) and (cge - |cge|) uses min(c, 0):
+// the eight upwind terms of umwm_advection.F90:40-47 (and the current terms
+// of :76-82) collapse to five coefficients times E* at the point and its four
+// unrolled neighbours.  The east/west neighbours sit about one wet column
+// (~nm points) away and are served from L2, which holds the window of blocks
+// the CTAs in flight work on.
+// Refraction needs E* at p-1 and p+1: inside a half they are registers, at
+// the half's edges they come from the partner lane (shuffle).  The rotation
+// rate is recomputed from cp0 and the currents (it depends on no spectral
+// value); when the reference would reuse the rotation of an earlier substep
 // (currents = .F.) the mask o <= oc of that substep is kept in oc_rot.
-// The wind stress sums e*Sin*cos/sin(th)/cp over the new spectrum while it
-// is still in registers and the last warp-group finishes the per-point
-// drag, skin-stress and ustar update.
+// The wind stress sums e*Sin*cos/sin(th)/cp over the new spectrum while it is
+// in registers; half 0 then finishes the drag, skin stress and ustar.
 #include "dev_common.cuh"
 #include "kernels.hpp"
 
 namespace umwm {
 
-constexpr int NW = 4;
+constexpr int PTS_A = 64;  // wet points per CTA (4 warps x 16)
 
 // stress_tail, umwm_stress.F90:300-311
 __device__ __forceinline__ float stress_tail(float w, float kmax) {
@@ -29,15 +34,32 @@ __device__ __forceinline__ float stress_tail(float w, float kmax) {
   return (powf(kcap, tail + 1.f) - kmax * kpt) / (kpt * (tail + 1.f));
 }
 
-template <int PW>
-__global__ void __launch_bounds__(128) k_advect(const Params prm, const Ptrs P) {
+// Sin at one direction (same expression as the source kernels)
+__device__ __forceinline__ float sin_dir(const Params& prm, const WindIn& w, float U, float cw, float ucs, float vss,
+                                         float cp0, float fkovg, bool tail) {
+  float s = U * cw - cp0 - ucs - vss;
+  s = (prm.sin_fac * fabsf(s)) * s;
+  if (s > 0.f) s = s * w.shelt_sf;
+  if (s < 0.f) {
+    s = s * prm.fieldscale1;
+    if (s < 0.f && cw > 0.f) s = s * prm.fieldscale2;
+  }
+  s = (w.c1 * s) * fkovg;
+  if (tail) s = fmaxf(s, 0.f);
+  return s;
+}
+
+template <int H, bool CURV>
+__global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs P) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int N = prm.N, ldN = prm.ldN, O = prm.O, NP = prm.P;
-  const int j = blockIdx.x * 32 + lane;
+  const int j16 = lane & 15, half = lane >> 4;
+  const int N = prm.N, O = prm.O;
+  const int j = blockIdx.x * PTS_A + w * 16 + j16;
   const bool valid = j < N;
   const int jj = valid ? j : N;
-  const int p0 = w * PW;
-  __shared__ float red[6][NW][32];
+  const float sg = half ? -1.f : 1.f;
+  __shared__ float cws[H][128];
+  __shared__ float ccs[CURV ? H : 1][128], scs[CURV ? H : 1][128];
 
   const Ctl* ctl = P.ctl;
   const float dta = ctl->dta, dtr = ctl->dtr;
@@ -51,137 +73,152 @@ __global__ void __launch_bounds__(128) k_advect(const Params prm, const Ptrs P) 
   const float ustar = P.ustar[jj];
   const WindIn wi = load_wind(prm, P, jj, ustar);
   const float wdir = P.wdir[jj];
+  const float ucg = sg * wi.uc, vcg = sg * wi.vc;
 
-  // current advection coefficients, umwm_advection.F90:64-74
-  float feup = 0.f, fedn = 0.f, fwup = 0.f, fwdn = 0.f, fnup = 0.f, fndn = 0.f, fsup = 0.f, fsdn = 0.f;
+  // current advection, umwm_advection.F90:62-82, folded per point
+  float F0 = 0.f, fedn = 0.f, fwup = 0.f, fndn = 0.f, fsup = 0.f;
   const float uci = P.uc[jj], vci = P.vc[jj];
-  const float uce = P.uc[P.iie[jj]], ucw = P.uc[P.iiw[jj]], ucn = P.uc[P.iin[jj]], ucs = P.uc[P.iis[jj]];
-  const float vce = P.vc[P.iie[jj]], vcw = P.vc[P.iiw[jj]], vcn = P.vc[P.iin[jj]], vcs = P.vc[P.iis[jj]];
+  const float ucn = P.uc[P.iin[jj]], ucs = P.uc[P.iis[jj]];
+  const float vce = P.vc[P.iie[jj]], vcw = P.vc[P.iiw[jj]];
   if (!zerocur) {
-    float ue = uci + uce, uw = uci + ucw, vn = vci + vcn, vs = vci + vcs;
-    feup = (ue + fabsf(ue)) * dye; fedn = (ue - fabsf(ue)) * dye;
-    fwup = (uw + fabsf(uw)) * dyw; fwdn = (uw - fabsf(uw)) * dyw;
-    fnup = (vn + fabsf(vn)) * dxn; fndn = (vn - fabsf(vn)) * dxn;
-    fsup = (vs + fabsf(vs)) * dxs; fsdn = (vs - fabsf(vs)) * dxs;
+    const float uce = P.uc[P.iie[jj]], ucw = P.uc[P.iiw[jj]], vcn = P.vc[P.iin[jj]], vcs = P.vc[P.iis[jj]];
+    const float ue = uci + uce, uw = uci + ucw, vn = vci + vcn, vs = vci + vcs;
+    const float feup = (ue + fabsf(ue)) * dye, fwdn = (uw - fabsf(uw)) * dyw;
+    const float fnup = (vn + fabsf(vn)) * dxn, fsdn = (vs - fabsf(vs)) * dxs;
+    fedn = (ue - fabsf(ue)) * dye; fwup = (uw + fabsf(uw)) * dyw;
+    fndn = (vn - fabsf(vn)) * dxn; fsup = (vs + fabsf(vs)) * dxs;
+    F0 = feup - fwdn + fnup - fsdn;
+  }
+  const float bx = (vce - vcw), by = (ucn - ucs);
+
+#pragma unroll
+  for (int k = 0; k < H; ++k) {
+    const float th = prm.th[half * H + k];
+    cws[k][threadIdx.x] = cosf(wdir - th);
+    if (CURV) {
+      const float cv = P.curv[jj];
+      ccs[k][threadIdx.x] = cosf(th + cv);
+      scs[k][threadIdx.x] = sinf(th + cv);
+    }
   }
 
-  float cw[PW], cc[PW], sc[PW];
-  const float cv = prm.curvilinear ? P.curv[jj] : 0.f;
-#pragma unroll
-  for (int k = 0; k < PW; ++k) {
-    const int p = p0 + k;
-    cw[k] = cosf(wdir - prm.th[p]);
-    if (prm.curvilinear) { cc[k] = cosf(prm.th[p] + cv); sc[k] = sinf(prm.th[p] + cv); }
-    else { cc[k] = prm.cth[p]; sc[k] = prm.sth[p]; }
-  }
+  // blocked-layout offsets of the point and its neighbours
+  const size_t lstride = (size_t)prm.NB * prm.P * 32;
+  const size_t tstride = (size_t)prm.NB * T_COUNT * 32;
+  const size_t hoff = (size_t)(half * H) * 32;
+  const size_t oS = sidx(prm, 0, 0, jj) + hoff, oE = sidx(prm, 0, 0, ie) + hoff, oW = sidx(prm, 0, 0, iw) + hoff,
+               oN = sidx(prm, 0, 0, in) + hoff, oSs = sidx(prm, 0, 0, is) + hoff;
   // stress_vector_integral divides by cp0 of the previous unrolled point
   // (assumed-shape dummy with lower bound 1 over cp0(:,0:im)),
   // umwm_stress.F90:401, :495-513
   const int jprev = (jj == 0 || jj >= N) ? N : jj - 1;
+  const size_t tS = tidx(prm, 0, 0, jj), tE = tidx(prm, 0, 0, ie), tW = tidx(prm, 0, 0, iw),
+               tN = tidx(prm, 0, 0, in), tSs = tidx(prm, 0, 0, is), tP = tidx(prm, 0, 0, jprev);
+  const float dtaq = 0.25f * dta * oneovar;
 
-  float sx = 0.f, sy = 0.f, dxs_ = 0.f, dys_ = 0.f, txom = 0.f, tyom = 0.f;
-  const int pm1 = (p0 + NP - 1) % NP, ppw = (p0 + PW) % NP;
+  float sx = 0.f, sy = 0.f, dsx = 0.f, dsy = 0.f, txom = 0.f, tyom = 0.f;
 
   for (int o = 0; o < O; ++o) {
-    const float* T = P.TAB + (size_t)o * T_COUNT * ldN;
-    const float* ESo = P.ES + (size_t)o * NP * ldN;
-    const float* EFo = P.EF + (size_t)o * NP * ldN;
-    float* Eo = P.E + (size_t)o * NP * ldN;
-    float ef[PW];
+    const float* T = P.TAB + (size_t)o * tstride;
+    const float* ESo = P.ES + (size_t)o * lstride;
+    const float* EFo = P.EF + (size_t)o * lstride;
+    float* Eo = P.E + (size_t)o * lstride;
+    float ef[H];
 #pragma unroll
-    for (int k = 0; k < PW; ++k) ef[k] = __ldg(EFo + (size_t)(p0 + k) * ldN + jj);
-    if (o < oc) {
+    for (int k = 0; k < H; ++k) ef[k] = __ldg(EFo + oS + k * 32);
+    const bool prog = o < oc;
+    const unsigned pm = __ballot_sync(0xffffffffu, prog);
+    if (prog) {
+      float es[H];
+#pragma unroll
+      for (int k = 0; k < H; ++k) es[k] = __ldg(ESo + oS + k * 32);
+      const float esm = __shfl_xor_sync(pm, es[H - 1], 16);  // E* at p-1 for k = 0
+      const float esp = __shfl_xor_sync(pm, es[0], 16);      // E* at p+1 for k = H-1
       // ---- propagation, umwm_advection.F90:30-97
-      const float* CG = T + T_CG0 * ldN;
-      const float cgi = __ldg(CG + jj), cgE = __ldg(CG + ie), cgW = __ldg(CG + iw), cgN = __ldg(CG + in),
-                  cgS = __ldg(CG + is);
-      float es[PW + 2];
-      es[0] = __ldg(ESo + (size_t)pm1 * ldN + jj);
+      const float cgi = __ldg(T + tS + T_CG0 * 32);
+      const float DE = 2.f * (cgi + __ldg(T + tE + T_CG0 * 32)) * dye;
+      const float DW = 2.f * (cgi + __ldg(T + tW + T_CG0 * 32)) * dyw;
+      const float DN = 2.f * (cgi + __ldg(T + tN + T_CG0 * 32)) * dxn;
+      const float DS = 2.f * (cgi + __ldg(T + tSs + T_CG0 * 32)) * dxs;
 #pragma unroll
-      for (int k = 0; k < PW; ++k) es[k + 1] = __ldg(ESo + (size_t)(p0 + k) * ldN + jj);
-      es[PW + 1] = __ldg(ESo + (size_t)ppw * ldN + jj);
-#pragma unroll
-      for (int k = 0; k < PW; ++k) {
-        const float* row = ESo + (size_t)(p0 + k) * ldN;
-        const float e0 = es[k + 1];
-        const float ee = __ldg(row + ie), ew = __ldg(row + iw), en = __ldg(row + in), esn = __ldg(row + is);
-        const float cge = cgi * cc[k] + cgE * cc[k];
-        const float cgw = cgi * cc[k] + cgW * cc[k];
-        const float cgs = cgi * sc[k] + cgS * sc[k];
-        const float cgn = cgi * sc[k] + cgN * sc[k];
-        float flux = (cge + fabsf(cge)) * dye * e0 + (cge - fabsf(cge)) * dye * ee -
-                     (cgw + fabsf(cgw)) * dyw * ew - (cgw - fabsf(cgw)) * dyw * e0 +
-                     (cgn + fabsf(cgn)) * dxn * e0 + (cgn - fabsf(cgn)) * dxn * en -
-                     (cgs + fabsf(cgs)) * dxs * esn - (cgs - fabsf(cgs)) * dxs * e0;
-        if (!zerocur)
-          flux = flux + (feup * e0 + fedn * ee - fwup * ew - fwdn * e0 + fnup * e0 + fndn * en - fsup * esn -
-                         fsdn * e0);
-        ef[k] = ef[k] - 0.25f * dta * flux * oneovar;
-        if (ice) ef[k] = 0.f;
+      for (int k = 0; k < H; ++k) {
+        const float e0 = es[k];
+        const float ee = __ldg(ESo + oE + k * 32), ew = __ldg(ESo + oW + k * 32);
+        const float en = __ldg(ESo + oN + k * 32), esn = __ldg(ESo + oSs + k * 32);
+        const float cc = CURV ? ccs[k][threadIdx.x] : sg * prm.cth[k];
+        const float sc = CURV ? scs[k][threadIdx.x] : sg * prm.sth[k];
+        const float cp = fmaxf(cc, 0.f), cm = fminf(cc, 0.f), sp = fmaxf(sc, 0.f), sm = fminf(sc, 0.f);
+        float flux = DE * (cp * e0 + cm * ee) - DW * (cp * ew + cm * e0) + DN * (sp * e0 + sm * en) -
+                     DS * (sp * esn + sm * e0);
+        if (!zerocur) flux += F0 * e0 + fedn * ee - fwup * ew + fndn * en - fsup * esn;
+        ef[k] = ice ? 0.f : ef[k] - dtaq * flux;
       }
       // ---- refraction, umwm_advection.F90:122-178
       if (o < ocr) {
-        const float* CP = T + T_CP0 * ldN;
-        const float dcx = __ldg(CP + ie) - __ldg(CP + iw);
-        const float dcy = __ldg(CP + in) - __ldg(CP + is);
-        float r[PW + 2];
+        const float gx = 0.5f * (__ldg(T + tE + T_CP0 * 32) - __ldg(T + tW + T_CP0 * 32));
+        const float gy = 0.5f * (__ldg(T + tN + T_CP0 * 32) - __ldg(T + tSs + T_CP0 * 32));
+        const float hbx = 0.5f * bx, hby = 0.5f * by;
+        // rotation rate at direction k of this half (sign sg) or of the partner half (-sg)
+        auto rot = [&](int k, float s) {
+          return (gx * s * prm.sth[k] + hbx) * odx - (gy * s * prm.cth[k] + hby) * ody;
+        };
+        float rprev = rot(H - 1, -sg);  // p-1 of k = 0 is the partner's last direction
+        float rcur = rot(0, sg);
 #pragma unroll
-        for (int k = 0; k < PW + 2; ++k) {
-          const int p = (k == 0) ? pm1 : (k == PW + 1 ? ppw : p0 + k - 1);
-          r[k] = 0.5f * ((dcx * prm.sth[p] + vce - vcw) * odx - (dcy * prm.cth[p] + ucn - ucs) * ody);
-        }
-#pragma unroll
-        for (int k = 0; k < PW; ++k) {
-          const float rl = 0.5f * (r[k + 1] + r[k + 2]);  // pl(p) = p+1
-          const float rr = 0.5f * (r[k + 1] + r[k]);      // pr(p) = p-1
-          const float fl = 0.5f *
-                           ((rl + fabsf(rl)) * es[k + 1] + (rl - fabsf(rl)) * es[k + 2] -
-                            (rr + fabsf(rr)) * es[k] - (rr - fabsf(rr)) * es[k + 1]) *
-                           prm.oneovdth;
-          ef[k] = ef[k] - dtr * fl;
-          if (ice) ef[k] = 0.f;
+        for (int k = 0; k < H; ++k) {
+          const float rnext = (k + 1 < H) ? rot(k + 1, sg) : rot(0, -sg);
+          const float rl = 0.5f * (rcur + rnext);  // pl(p) = p+1
+          const float rr = 0.5f * (rcur + rprev);  // pr(p) = p-1
+          const float el = (k + 1 < H) ? es[k + 1] : esp;
+          const float er = (k > 0) ? es[k - 1] : esm;
+          const float fl = (fmaxf(rl, 0.f) * es[k] + fminf(rl, 0.f) * el - fmaxf(rr, 0.f) * er -
+                            fminf(rr, 0.f) * es[k]) * prm.oneovdth;
+          ef[k] = ice ? 0.f : ef[k] - dtr * fl;
+          rprev = rcur;
+          rcur = rnext;
         }
       }
     }
-    // ---- e = ef and the form-stress integrand
-    const float logl2z = __ldg(T + T_LOGL2Z * ldN + jj), cp0 = __ldg(T + T_CP0 * ldN + jj);
-    const float fkovg = __ldg(T + T_FKOVG * ldN + jj), kdk = __ldg(T + T_KDK * ldN + jj);
-    const float icp = 1.f / __ldg(T + T_CP0 * ldN + jprev);
-    const bool tail = o >= oc;
+    // ---- e = ef, and the form-stress integrand with the new spectrum
+    const float U = wi.wspd + wi.ustar25 * __ldg(T + tS + T_LOGL2Z * 32);
+    const float cp0 = __ldg(T + tS + T_CP0 * 32), fkovg = __ldg(T + tS + T_FKOVG * 32);
+    const float kdk = __ldg(T + tS + T_KDK * 32);
+    const float icp = 1.f / __ldg(T + tP + T_CP0 * 32);
+    const bool tail = !prog;
     float tx = 0.f, ty = 0.f;
 #pragma unroll
-    for (int k = 0; k < PW; ++k) {
-      const int p = p0 + k;
-      if (valid) Eo[(size_t)p * ldN + j] = ef[k];
-      float s = sin_bin(prm, wi, cw[k], prm.cth[p], prm.sth[p], logl2z, cp0, fkovg, tail);
-      float es_ = ef[k] * s;
-      tx += es_ * prm.cth[p] * icp;
-      ty += es_ * prm.sth[p] * icp;
+    for (int k = 0; k < H; ++k) {
+      if (valid) Eo[oS + k * 32] = ef[k];
+      const float s = sin_dir(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], cp0, fkovg, tail);
+      const float es_ = ef[k] * s;
+      tx += es_ * prm.cth[k];
+      ty += es_ * prm.sth[k];
     }
+    tx *= sg * icp;
+    ty *= sg * icp;
     sx += tx * kdk; sy += ty * kdk;
-    if (o >= oc - 1) { dxs_ += tx * kdk; dys_ += ty * kdk; }
+    if (o >= oc - 1) { dsx += tx * kdk; dsy += ty * kdk; }
     if (o == O - 1) { txom = tx; tyom = ty; }
   }
-
-  red[0][w][lane] = sx; red[1][w][lane] = sy; red[2][w][lane] = dxs_;
-  red[3][w][lane] = dys_; red[4][w][lane] = txom; red[5][w][lane] = tyom;
-  __syncthreads();
-  if (w != 0 || !valid) return;
-  float v[6];
-#pragma unroll
-  for (int q = 0; q < 6; ++q) v[q] = ((red[q][0][lane] + red[q][1][lane]) + red[q][2][lane]) + red[q][3][lane];
+  sx += __shfl_xor_sync(0xffffffffu, sx, 16);
+  sy += __shfl_xor_sync(0xffffffffu, sy, 16);
+  dsx += __shfl_xor_sync(0xffffffffu, dsx, 16);
+  dsy += __shfl_xor_sync(0xffffffffu, dsy, 16);
+  txom += __shfl_xor_sync(0xffffffffu, txom, 16);
+  tyom += __shfl_xor_sync(0xffffffffu, tyom, 16);
+  if (half != 0 || !valid) return;
   // ---- stress('atm') per point, umwm_stress.F90:216-262
   const float rhow = P.rhow[j], rhoa = P.rhoa[j], wspd = wi.wspd;
-  const float kom = __ldg(P.TAB + ((size_t)(O - 1) * T_COUNT + T_K) * ldN + j);
-  const float tail = stress_tail(wspd, kom);
-  const float tax = v[4] * kom * tail * rhow * prm.dthg;
-  const float tay = v[5] * kom * tail * rhow * prm.dthg;
-  const float tfx = v[0] * rhow * prm.dthg + tax;
-  const float tfy = v[1] * rhow * prm.dthg + tay;
+  const float kom = __ldg(P.TAB + (size_t)(O - 1) * tstride + tS + T_K * 32);
+  const float tl = stress_tail(wspd, kom);
+  const float tax = txom * kom * tl * rhow * prm.dthg;
+  const float tay = tyom * kom * tl * rhow * prm.dthg;
+  const float tfx = sx * rhow * prm.dthg + tax;
+  const float tfy = sy * rhow * prm.dthg + tay;
   P.tailatmx[j] = tax; P.tailatmy[j] = tay;
   P.taux_form[j] = tfx; P.tauy_form[j] = tfy;
-  P.taux_diag[j] = v[2] * rhow * prm.dthg;
-  P.tauy_diag[j] = v[3] * rhow * prm.dthg;
+  P.taux_diag[j] = dsx * rhow * prm.dthg;
+  P.tauy_diag[j] = dsy * rhow * prm.dthg;
   const float us1 = prm.lm > 0 ? P.us[j] : 0.f, vs1 = prm.lm > 0 ? P.vs[j] : 0.f;
   const float urel = wspd * cosf(wdir) - (uci + us1);
   const float vrel = wspd * sinf(wdir) - (vci + vs1);
@@ -207,12 +244,15 @@ __global__ void __launch_bounds__(128) k_advect(const Params prm, const Ptrs P) 
 }
 
 cudaError_t launch_advect(const Params& prm, const Ptrs& P, cudaStream_t st) {
-  const int PW = prm.P / NW;
-  dim3 grid((prm.N + 31) / 32), block(128);
-  switch (PW) {
-#define CASE(X) \
-  case X: k_advect<X><<<grid, block, 0, st>>>(prm, P); break;
-    CASE(2) CASE(3) CASE(4) CASE(6) CASE(8) CASE(9) CASE(12) CASE(16) CASE(18)
+  dim3 grid((prm.N + PTS_A - 1) / PTS_A), block(128);
+  const bool curv = prm.curvilinear != 0;
+  switch (prm.P / 2) {
+#define CASE(X)                                                          \
+  case X:                                                                \
+    if (curv) k_advect<X, true><<<grid, block, 0, st>>>(prm, P);         \
+    else k_advect<X, false><<<grid, block, 0, st>>>(prm, P);             \
+    break;
+    CASE(4) CASE(6) CASE(8) CASE(12) CASE(16) CASE(18) CASE(24)
 #undef CASE
     default: return cudaErrorInvalidConfiguration;
   }

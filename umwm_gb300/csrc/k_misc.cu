@@ -86,7 +86,7 @@ __global__ void k_sice(const Params prm, const Ptrs P) {
     float h = 0.f;
     for (int p = 0; p < prm.P; ++p)
       for (int o = 0; o < prm.O; ++o)
-        h += P.E[((size_t)o * prm.P + p) * prm.ldN + j] * P.TAB[((size_t)o * T_COUNT + T_KDK) * prm.ldN + j];
+        h += P.E[sidx(prm, o, p, j)] * P.TAB[tidx(prm, o, T_KDK, j)];
     h = 4.f * sqrtf(h * prm.dth);
     const float C1 = -5.35e-6f;
     sv = (h < 3.f) ? C1 * h : C1 * 3.f;
@@ -98,9 +98,9 @@ __global__ void k_sice(const Params prm, const Ptrs P) {
 __global__ void k_diag(const Params prm, const Ptrs P) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= prm.N) return;
-  const int O = prm.O, NP = prm.P, ldN = prm.ldN, oc = P.oc[j];
+  const int O = prm.O, NP = prm.P, oc = P.oc[j];
   const float* E = P.E;
-  auto tab = [&](int t, int o) { return P.TAB[((size_t)o * T_COUNT + t) * ldN + j]; };
+  auto tab = [&](int t, int o) { return P.TAB[tidx(prm, o, t, j)]; };
   float m0 = 0.f, m2 = 0.f, m2k = 0.f, mx = 0.f, my = 0.f, cxx = 0.f, cxy = 0.f, cyy = 0.f, xc = 0.f, yc = 0.f;
   float best = -1.f;
   int op = 0, pp = 0;
@@ -108,7 +108,7 @@ __global__ void k_diag(const Params prm, const Ptrs P) {
     float mag = 0.f;
     const float cth = prm.cth[p], sth = prm.sth[p];
     for (int o = 0; o < O; ++o) {
-      const float e = E[((size_t)o * NP + p) * ldN + j];
+      const float e = E[sidx(prm, o, p, j)];
       const float kdk = tab(T_KDK, o);
       const float ek = e * kdk;
       m0 += ek;
@@ -153,7 +153,7 @@ __global__ void k_stokes(const Params prm, const Ptrs P) {
   for (int o = 0; o < O; ++o) {
     float x = 0.f, y = 0.f;
     for (int p = 0; p < NP; ++p) {
-      const float e = P.E[((size_t)o * NP + p) * ldN + j];
+      const float e = P.E[sidx(prm, o, p, j)];
       x += e * prm.cth[p];
       y += e * prm.sth[p];
     }
@@ -168,8 +168,8 @@ __global__ void k_stokes(const Params prm, const Ptrs P) {
     float su = 0.f, sv = 0.f;
     if (!(fabsf(dep) > d)) {
       for (int o = 0; o < O; ++o) {
-        const float kk = P.TAB[((size_t)o * T_COUNT + T_K) * ldN + j];
-        const float dwn = prm.dom[o] / fabsf(P.TAB[((size_t)o * T_COUNT + T_CG0) * ldN + j]);
+        const float kk = P.TAB[tidx(prm, o, T_K, j)];
+        const float dwn = prm.dom[o] / fabsf(P.TAB[tidx(prm, o, T_CG0, j)]);
         const float kd = kk * d;
         const float arg = 2.f * kk * (dep + d);
         float u;
@@ -207,8 +207,8 @@ __global__ void k_screen(const Params prm, const Ptrs P) {
   float a = 0.f, b = 0.f;
   if (j >= 0) {
     for (int b_ = threadIdx.x; b_ < prm.O * prm.P; b_ += blockDim.x) {
-      const int o = b_ / prm.P;
-      const float ek = P.E[(size_t)b_ * prm.ldN + j] * P.TAB[((size_t)o * T_COUNT + T_KDK) * prm.ldN + j];
+      const int o = b_ / prm.P, p = b_ % prm.P;
+      const float ek = P.E[sidx(prm, o, p, j)] * P.TAB[tidx(prm, o, T_KDK, j)];
       a += ek;
       b += (prm.f[o] * prm.f[o]) * ek;
     }
@@ -239,7 +239,7 @@ __global__ void k_screen(const Params prm, const Ptrs P) {
   }
 }
 
-// Reference order F(om,pm,im) (o fastest) <-> device [o][p][ldN].
+// Reference order F(om,pm,im) (o fastest) <-> the blocked device layout.
 __global__ void k_to_ref(const Params prm, const float* __restrict__ E, float* __restrict__ F) {
   __shared__ float tile[32][33];
   const int R = prm.O * prm.P;
@@ -249,7 +249,7 @@ __global__ void k_to_ref(const Params prm, const float* __restrict__ E, float* _
     const int c = c0 + k;  // column of F: c = p*O + o
     if (c < R && j0 + tx < prm.N) {
       const int o = c % prm.O, p = c / prm.O;
-      tile[k][tx] = E[((size_t)o * prm.P + p) * prm.ldN + j0 + tx];
+      tile[k][tx] = E[sidx(prm, o, p, j0 + tx)];
     }
   }
   __syncthreads();
@@ -273,7 +273,7 @@ __global__ void k_from_ref(const Params prm, const float* __restrict__ F, float*
     const int c = c0 + k;
     if (c < R && j0 + tx < prm.N) {
       const int o = c % prm.O, p = c / prm.O;
-      E[((size_t)o * prm.P + p) * prm.ldN + j0 + tx] = tile[tx][k];
+      E[sidx(prm, o, p, j0 + tx)] = tile[tx][k];
     }
   }
 }

@@ -1,22 +1,28 @@
 // Source-term kernels: sin_d12, sds_d12, snl_d12, s_ice and source()
 // (umwm_source_functions.F90:16-183, umwm_physics.F90:9-86).
 //
-// One CTA owns a tile of 32 consecutive wet points (lane = point, so every
-// load of one (o,p) bin is a 128-byte line) and 4 warps split the pm
-// directions into 4 contiguous groups of PW.  The frequency loop walks
-// o = 1..om in order because the mean-square-slope adjustment of Sds is a
-// prefix over o:
+// Thread mapping.  A warp owns 16 consecutive wet points; lane = point +
+// 16 * half, where half 0 takes directions p = 0..H-1 and half 1 takes
+// p = H..2H-1 (H = pm/2).  Direction p+H is direction p turned by pi, so
+// cos/sin(th) flip sign and cos/sin(2 th) are equal: both halves run the same
+// code with the direction index k = 0..H-1 known at compile time (every
+// direction constant is an immediate operand), with a per-lane sign.  Both
+// halves of a point combine their partial sums with one shuffle.
+//
+// The frequency loop walks o = 1..om in order because the mean-square-slope
+// adjustment of Sds is a prefix over o:
 //   dummy(o,p) = dummy(o-1,p) + k3dk(o-1) * sum_pp e(o-1,pp) cth2pp(pp,p),
-//   cth2pp(pp,p) = cos^2(th(pp)-th(p)) dth = dth/2 (1 + cos2th(pp)cos2th(p)
-//                                                  + sin2th(pp)sin2th(p)),
+//   cth2pp(pp,p) = cos^2(th(pp)-th(p)) dth
+//                = dth/2 (1 + cos2th(pp)cos2th(p) + sin2th(pp)sin2th(p)),
 // so dummy(o,.) = A + B cos2th(p) + C sin2th(p) with three running sums per
-// point (exact algebra; replaces pm multiply-adds per bin by 2).
+// point (exact algebra; two multiply-adds per bin instead of pm).
 // Snl at level o needs Sds*e at o+1 and o+2, so the integration finishes
-// level o two iterations after it was loaded.
+// level o two levels after it was loaded (registers hold two levels of e and
+// Sds per direction).  Upcoming levels are prefetched into L2.
 //
 // MODE_PHYS : per-point max |exponent argument| -> physics_time_step and the
-//             global min for dts (umwm_physics.F90:18-41); optionally the
-//             global max of the rotation rate for refraction's dtr
+//             global min for dts (umwm_physics.F90:18-41); with compute_rot
+//             also the global max of the rotation rate for refraction's dtr
 //             (umwm_advection.F90:125-154).
 // MODE_INTEG: exponential integration (o <= oc), equilibrium tail (o > oc),
 //             E* = (e + ef)/2 -> ES, ef -> EF (umwm_physics.F90:61-84).
@@ -25,18 +31,79 @@
 
 namespace umwm {
 
-constexpr int NWARP = 4;
+constexpr int PTS = 64;  // wet points per CTA (4 warps x 16)
 
-template <int PW, bool INTEG>
-__global__ void __launch_bounds__(128) k_source(const Params prm, const Ptrs P, int compute_rot) {
+// bulk prefetch of a contiguous, 16-byte aligned range into L2 (sizes are multiples of 16 bytes)
+__device__ __forceinline__ void bulk_prefetch_l2(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ float ex2a(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2a(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// x^y for x >= 0 (0 for x == 0)
+__device__ __forceinline__ float powp(float x, float y) { return ex2a(y * lg2a(x)); }
+
+template <int H>
+struct Level {  // per-(o, point) inputs of one frequency level
+  float k4, logl2z, cp0, fkovg, cothkd, sbf, sdv, kk, bf1r, bf2r, cg0, k3dk;
+};
+struct Coef {  // dummy coefficients A + B cos2th + C sin2th of one level
+  float a, b, c;
+};
+
+// T points at table row 0 of this point's block and frequency
+template <int H>
+__device__ __forceinline__ Level<H> load_level(const Params& prm, const float* T, bool full) {
+  Level<H> L;
+  L.k4 = __ldg(T + T_K4 * 32);
+  L.k3dk = __ldg(T + T_K3DK * 32);
+  if (full) {
+    L.logl2z = __ldg(T + T_LOGL2Z * 32);
+    L.cp0 = __ldg(T + T_CP0 * 32);
+    L.fkovg = __ldg(T + T_FKOVG * 32);
+    L.cothkd = __ldg(T + T_COTHKD * 32);
+    L.sbf = __ldg(T + T_SBF * 32);
+    L.sdv = __ldg(T + T_SDV * 32);
+    L.kk = __ldg(T + T_K * 32);
+    L.bf1r = __ldg(T + T_BF1R * 32);
+    L.bf2r = __ldg(T + T_BF2R * 32);
+    L.cg0 = prm.ice_possible ? __ldg(T + T_CG0 * 32) : 0.f;
+  }
+  return L;
+}
+
+// Sin at direction k of this half; cw = cos(wdir - th(p)) from shared memory.
+__device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float U, float cw, float ucs, float vss,
+                                       float cp0, float fkovg, bool tail) {
+  float s = U * cw - cp0 - ucs - vss;
+  s = (prm.sin_fac * fabsf(s)) * s;
+  if (s > 0.f) s = s * w.shelt_sf;
+  if (s < 0.f) {
+    s = s * prm.fieldscale1;
+    if (s < 0.f && cw > 0.f) s = s * prm.fieldscale2;
+  }
+  s = (w.c1 * s) * fkovg;
+  if (tail) s = fmaxf(s, 0.f);
+  return s;
+}
+
+template <int H, bool INTEG>
+__global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm, const Ptrs P, int compute_rot) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int N = prm.N, ldN = prm.ldN, O = prm.O, NP = prm.P;
-  const int j = blockIdx.x * 32 + lane;
+  const int j16 = lane & 15, half = lane >> 4;
+  const int N = prm.N, O = prm.O;
+  const int j = blockIdx.x * PTS + w * 16 + j16;
   const bool valid = j < N;
   const int jj = valid ? j : N;  // the ghost column keeps loads in bounds
-  const int p0 = w * PW;
-  __shared__ float4 part[2][NWARP][32];
-  __shared__ float red[NWARP][32];
+  const float sg = half ? -1.f : 1.f;
+  __shared__ float cws[H][128];
 
   const float dts = INTEG ? P.ctl->dts : 0.f;
   const float ustar = P.ustar[jj];
@@ -45,12 +112,11 @@ __global__ void __launch_bounds__(128) k_source(const Params prm, const Ptrs P, 
   const float sdtc = (prm.sdt_fac * sqrtf(P.rhorat[jj])) * ustar;
   const float sv = prm.ice_possible ? P.sice_v[jj] : 0.f;
   const float hdth = 0.5f * prm.dth;
-
-  float cw[PW];
+  const float ucg = sg * wi.uc, vcg = sg * wi.vc;
 #pragma unroll
-  for (int k = 0; k < PW; ++k) cw[k] = cosf(wdir - prm.th[p0 + k]);
+  for (int k = 0; k < H; ++k) cws[k][threadIdx.x] = cosf(wdir - prm.th[half * H + k]);
+  // own bins only: no barrier needed (each thread reads its own column)
 
-  // rotation-rate inputs (refraction), only for MODE_PHYS with compute_rot
   int nie = N, niw = N, nin = N, nis = N;
   float vce = 0.f, vcw = 0.f, ucn = 0.f, ucs = 0.f, odx = 0.f, ody = 0.f;
   if (!INTEG && compute_rot) {
@@ -59,175 +125,164 @@ __global__ void __launch_bounds__(128) k_source(const Params prm, const Ptrs P, 
     odx = P.oneovdx[jj]; ody = P.oneovdy[jj];
   }
 
-  float A = 0.f, B = 0.f, C = 0.f;        // dummy coefficients for the current level
-  float A2 = 0.f, B2 = 0.f, C2 = 0.f;     // ... two levels back (tail of MODE_INTEG)
-  float A1 = 0.f, B1 = 0.f, C1 = 0.f;     // ... one level back
-  float eL1[PW], eL2[PW], sL1[PW], sL2[PW];
-#pragma unroll
-  for (int k = 0; k < PW; ++k) { eL1[k] = eL2[k] = sL1[k] = sL2[k] = 0.f; }
-  float mx = 0.f, rmx = 0.f;
+  // level strides of the blocked layouts
+  const size_t lstride = (size_t)prm.NB * prm.P * 32;
+  const size_t tstride = (size_t)prm.NB * T_COUNT * 32;
+  const float* Eb = P.E + sidx(prm, 0, half * H, jj);
+  const float* Tb = P.TAB + tidx(prm, 0, 0, jj);
+  const float* Eblk = P.E + sidx(prm, 0, 0, jj & ~31);  // start of this block's region
+  auto pf = [&](int o) {
+    if (o < O && lane == 0) bulk_prefetch_l2(Eblk + (size_t)o * lstride, (unsigned)(prm.P * 128));
+  };
+  pf(0);
+  pf(1);
 
-  const int OL = INTEG ? O + 2 : O;
-  for (int o = 0; o < OL; ++o) {
-    float ec[PW], sc[PW];
-    if (o < O) {
-      const float* Erow = P.E + ((size_t)o * NP + p0) * ldN + jj;
+  float A = 0.f, B = 0.f, C = 0.f;  // dummy coefficients of the current level
+  float mx = 0.f, rmx = 0.f;
+  // three rotating buffers: level o lives in buffer o % 3
+  float eX[H], eY[H], eZ[H], sX[H], sY[H], sZ[H];
 #pragma unroll
-      for (int k = 0; k < PW; ++k) ec[k] = __ldg(Erow + (size_t)k * ldN);
-      const float* T = P.TAB + (size_t)o * T_COUNT * ldN + jj;
-      const float k4 = __ldg(T + T_K4 * ldN);
+  for (int k = 0; k < H; ++k) { eX[k] = eY[k] = eZ[k] = sX[k] = sY[k] = sZ[k] = 0.f; }
+  Coef CX{}, CY{}, CZ{};
+
+  // one frequency level o: load and Sds of level o into (ec, sc, Lc); in
+  // MODE_INTEG finish level o-2 whose values are in (e2, s2, L2), with the
+  // Snl partners at o-1 in (e1, s1)
+  auto step = [&](int o, float (&ec)[H], float (&sc)[H], Coef& Cc, const float (&e1)[H], const float (&s1)[H],
+                  const float (&e2)[H], const float (&s2)[H], const Coef& C2) {
+    pf(o + 2);
+    if (o < O) {
+      const float* r = Eb + (size_t)o * lstride;
+#pragma unroll
+      for (int k = 0; k < H; ++k) ec[k] = __ldg(r + k * 32);
+      const bool prog = o < wi.oc;
+      const Level<H> Lc = load_level<H>(prm, Tb + (size_t)o * tstride, !INTEG && prog);
+      Cc.a = A; Cc.b = B; Cc.c = C;
       float s0 = 0.f, sc2 = 0.f, ss2 = 0.f;
 #pragma unroll
-      for (int k = 0; k < PW; ++k) {
+      for (int k = 0; k < H; ++k) {
         s0 += ec[k];
-        sc2 += ec[k] * prm.c2th[p0 + k];
-        ss2 += ec[k] * prm.s2th[p0 + k];
+        sc2 += ec[k] * prm.c2th[k];
+        ss2 += ec[k] * prm.s2th[k];
       }
-      part[o & 1][w][lane] = make_float4(s0, sc2, ss2, 0.f);
+      s0 += __shfl_xor_sync(0xffffffffu, s0, 16);
+      sc2 += __shfl_xor_sync(0xffffffffu, sc2, 16);
+      ss2 += __shfl_xor_sync(0xffffffffu, ss2, 16);
       const float sA = prm.twopisds_fac * prm.f[o];
+      if (INTEG || prog) {
 #pragma unroll
-      for (int k = 0; k < PW; ++k) {
-        float chi = A + B * prm.c2th[p0 + k] + C * prm.s2th[p0 + k];
-        float t = 1.f + prm.mss_fac * chi;
-        sc[k] = (sA * (t * t)) * pow_pos(ec[k] * k4, prm.sds_power);
+        for (int k = 0; k < H; ++k) {
+          const float chi = A + B * prm.c2th[k] + C * prm.s2th[k];
+          const float t = 1.f + prm.mss_fac * chi;
+          sc[k] = (sA * (t * t)) * powp(ec[k] * Lc.k4, prm.sds_power);
+        }
       }
-      if (!INTEG) {
-        if (o < wi.oc) {
-          const float logl2z = __ldg(T + T_LOGL2Z * ldN), cp0 = __ldg(T + T_CP0 * ldN);
-          const float fkovg = __ldg(T + T_FKOVG * ldN), cothkd = __ldg(T + T_COTHKD * ldN);
-          const float sbf = __ldg(T + T_SBF * ldN), sdv = __ldg(T + T_SDV * ldN), kk = __ldg(T + T_K * ldN);
-          const float snl_arg = 1.f - (__ldg(T + T_BF1R * ldN) + __ldg(T + T_BF2R * ldN));
-          const float sdt = sdtc * kk;
-          const float sice = sv != 0.f ? 2.f * __ldg(T + T_CG0 * ldN) * sv : 0.f;
+      if (!INTEG && prog) {
+        const float U = wi.wspd + wi.ustar25 * Lc.logl2z;
+        const float snl_arg = 1.f - (Lc.bf1r + Lc.bf2r);
+        const float cs = Lc.cothkd * snl_arg;
+        const float sink = Lc.sbf + sdtc * Lc.kk + Lc.sdv - (sv != 0.f ? 2.f * Lc.cg0 * sv : 0.f);
 #pragma unroll
-          for (int k = 0; k < PW; ++k) {
-            const int p = p0 + k;
-            float s = sin_bin(prm, wi, cw[k], prm.cth[p], prm.sth[p], logl2z, cp0, fkovg, false);
-            float a = s - (sc[k] * cothkd) * snl_arg - sbf - sdt - sdv + sice;
-            mx = fmaxf(mx, fabsf(a));
-          }
-          if (compute_rot) {
-            const float* CP = P.TAB + ((size_t)o * T_COUNT + T_CP0) * ldN;
-            const float dcx = __ldg(CP + nie) - __ldg(CP + niw);
-            const float dcy = __ldg(CP + nin) - __ldg(CP + nis);
+        for (int k = 0; k < H; ++k) {
+          const float s = sin_k(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], Lc.cp0,
+                                Lc.fkovg, false);
+          mx = fmaxf(mx, fabsf(s - sc[k] * cs - sink));
+        }
+        if (compute_rot) {
+          const float* CP = P.TAB + (size_t)o * tstride + T_CP0 * 32;
+          const float dcx = __ldg(CP + tidx(prm, 0, 0, nie)) - __ldg(CP + tidx(prm, 0, 0, niw));
+          const float dcy = __ldg(CP + tidx(prm, 0, 0, nin)) - __ldg(CP + tidx(prm, 0, 0, nis));
+          const float gx = sg * dcx, gy = sg * dcy;
 #pragma unroll
-            for (int k = 0; k < PW; ++k) {
-              const int p = p0 + k;
-              float r = 0.5f * ((dcx * prm.sth[p] + vce - vcw) * odx - (dcy * prm.cth[p] + ucn - ucs) * ody);
-              rmx = fmaxf(rmx, r);
-            }
+          for (int k = 0; k < H; ++k) {
+            const float rr = 0.5f * ((gx * prm.sth[k] + vce - vcw) * odx - (gy * prm.cth[k] + ucn - ucs) * ody);
+            rmx = fmaxf(rmx, rr);
           }
         }
       }
+      const float hk = Lc.k3dk * hdth;
+      A += hk * s0; B += hk * sc2; C += hk * ss2;
     } else {
 #pragma unroll
-      for (int k = 0; k < PW; ++k) { ec[k] = 0.f; sc[k] = 0.f; }
+      for (int k = 0; k < H; ++k) { ec[k] = 0.f; sc[k] = 0.f; }
     }
-    __syncthreads();
-    float S0 = 0.f, SC = 0.f, SS = 0.f;
-    if (o < O) {
-#pragma unroll
-      for (int q = 0; q < NWARP; ++q) {
-        float4 v = part[o & 1][q][lane];
-        S0 += v.x; SC += v.y; SS += v.z;
-      }
-    }
-    if (INTEG && o >= 2) {
-      // finish level L = o-2
-      const int L = o - 2;
-      const float* T = P.TAB + (size_t)L * T_COUNT * ldN + jj;
-      const float logl2z = __ldg(T + T_LOGL2Z * ldN), cp0 = __ldg(T + T_CP0 * ldN);
-      const float fkovg = __ldg(T + T_FKOVG * ldN), cothkd = __ldg(T + T_COTHKD * ldN);
-      const float sbf = __ldg(T + T_SBF * ldN), sdv = __ldg(T + T_SDV * ldN), kk = __ldg(T + T_K * ldN);
-      const float sdt = sdtc * kk;
-      const float sice = sv != 0.f ? 2.f * __ldg(T + T_CG0 * ldN) * sv : 0.f;
-      const bool prog = L < wi.oc;
-      float* ESrow = P.ES + ((size_t)L * NP + p0) * ldN + j;
-      float* EFrow = P.EF + ((size_t)L * NP + p0) * ldN + j;
+    if (INTEG && o >= 2 && o < O + 2) {
+      const int Lv = o - 2;
+      const bool prog = Lv < wi.oc;
+      const Level<H> L2 = load_level<H>(prm, Tb + (size_t)Lv * tstride, true);
+      const float U = wi.wspd + wi.ustar25 * L2.logl2z;
+      const float sdt = sdtc * L2.kk;
+      const float sice = sv != 0.f ? 2.f * L2.cg0 * sv : 0.f;
+      float* ES = P.ES + sidx(prm, 0, half * H, jj) + (size_t)Lv * lstride;
+      float* EF = P.EF + sidx(prm, 0, half * H, jj) + (size_t)Lv * lstride;
       if (prog) {
-        const float bf1r = __ldg(T + T_BF1R * ldN), bf2r = __ldg(T + T_BF2R * ldN);
 #pragma unroll
-        for (int k = 0; k < PW; ++k) {
-          const int p = p0 + k;
-          float s = sin_bin(prm, wi, cw[k], prm.cth[p], prm.sth[p], logl2z, cp0, fkovg, false);
-          float snl = (bf1r * sL1[k]) * eL1[k] + (bf2r * sc[k]) * ec[k] - (prm.snl_fac * sL2[k]) * eL2[k];
-          float S = s - sL2[k] * cothkd - sbf - sdt - sdv + sice;
-          float ef = eL2[k] * __expf(dts * S) + dts * snl;
+        for (int k = 0; k < H; ++k) {
+          const float s = sin_k(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0,
+                                L2.fkovg, false);
+          const float snl = (L2.bf1r * s1[k]) * e1[k] + (L2.bf2r * sc[k]) * ec[k] - (prm.snl_fac * s2[k]) * e2[k];
+          const float S = s - s2[k] * L2.cothkd - L2.sbf - sdt - L2.sdv + sice;
+          const float ef = e2[k] * ex2a(dts * S * 1.44269504f) + dts * snl;
           if (valid) {
-            ESrow[(size_t)k * ldN] = 0.5f * (eL2[k] + ef);
-            EFrow[(size_t)k * ldN] = ef;
+            ES[k * 32] = 0.5f * (e2[k] + ef);
+            EF[k * 32] = ef;
           }
         }
       } else {
-        const float oneoverk4 = 1.f / __ldg(T + T_K4 * ldN);
-        const float sAc = (prm.twopisds_fac * prm.f[L]);
+        const float oneoverk4 = 1.f / L2.k4;
+        const float sAc = prm.twopisds_fac * prm.f[Lv];
 #pragma unroll
-        for (int k = 0; k < PW; ++k) {
-          const int p = p0 + k;
-          float s = sin_bin(prm, wi, cw[k], prm.cth[p], prm.sth[p], logl2z, cp0, fkovg, true);
-          float num = s - sdt - sdv + sice;
+        for (int k = 0; k < H; ++k) {
+          const float s = sin_k(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0,
+                                L2.fkovg, true);
+          const float num = s - sdt - L2.sdv + sice;
           float ef = 0.f;
           if (num >= 0.f) {
-            float chi = A2 + B2 * prm.c2th[p] + C2 * prm.s2th[p];
-            float t = 1.f + prm.mss_fac * chi;
-            float den = (sAc * (t * t)) * cothkd;
-            ef = oneoverk4 * pow_pos(num / den, prm.inv_sds_power);
+            const float chi = C2.a + C2.b * prm.c2th[k] + C2.c * prm.s2th[k];
+            const float t = 1.f + prm.mss_fac * chi;
+            const float den = (sAc * (t * t)) * L2.cothkd;
+            ef = oneoverk4 * powp(num / den, prm.inv_sds_power);
           }
           if (valid) {
-            ESrow[(size_t)k * ldN] = 0.5f * (eL2[k] + ef);
-            EFrow[(size_t)k * ldN] = ef;
+            ES[k * 32] = 0.5f * (e2[k] + ef);
+            EF[k * 32] = ef;
           }
         }
       }
     }
-    // advance the dummy coefficients: level o -> o+1
-    A2 = A1; B2 = B1; C2 = C1;
-    A1 = A; B1 = B; C1 = C;
-    if (o < O) {
-      const float h = __ldg(P.TAB + ((size_t)o * T_COUNT + T_K3DK) * ldN + jj) * hdth;
-      A += h * S0; B += h * SC; C += h * SS;
-    }
-    if (INTEG) {
-#pragma unroll
-      for (int k = 0; k < PW; ++k) { eL2[k] = eL1[k]; sL2[k] = sL1[k]; eL1[k] = ec[k]; sL1[k] = sc[k]; }
-    }
+  };
+
+  const int OL = INTEG ? O + 2 : O;
+  for (int o = 0; o < OL; o += 3) {
+    step(o, eX, sX, CX, eZ, sZ, eY, sY, CY);
+    if (o + 1 < OL) step(o + 1, eY, sY, CY, eX, sX, eZ, sZ, CZ);
+    if (o + 2 < OL) step(o + 2, eZ, sZ, CZ, eY, sY, eX, sX, CX);
   }
 
   if (!INTEG) {
-    // per-point max over the 4 direction groups, then explim / max
-    red[w][lane] = mx;
-    __syncthreads();
-    if (w == 0) {
-      float m = fmaxf(fmaxf(red[0][lane], red[1][lane]), fmaxf(red[2][lane], red[3][lane]));
-      float ph = prm.explim / m;
-      if (valid) P.phys[j] = ph;
-      float bm = valid ? ph : __int_as_float(0x7f800000);
+    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+    float ph = prm.explim / mx;
+    if (valid && half == 0) P.phys[j] = ph;
+    float bm = valid ? ph : __int_as_float(0x7f800000);
 #pragma unroll
-      for (int s = 16; s > 0; s >>= 1) bm = fminf(bm, __shfl_xor_sync(0xffffffffu, bm, s));
-      if (lane == 0) atomicMin(&P.ctl->minphys_enc, enc_ord_d(bm));
-    }
+    for (int s = 8; s > 0; s >>= 1) bm = fminf(bm, __shfl_xor_sync(0xffffffffu, bm, s));
+    if (lane == 0) atomicMin(&P.ctl->minphys_enc, enc_ord_d(bm));
     if (compute_rot) {
-      __syncthreads();
-      red[w][lane] = valid ? rmx : 0.f;
-      __syncthreads();
-      if (w == 0) {
-        float m = fmaxf(fmaxf(red[0][lane], red[1][lane]), fmaxf(red[2][lane], red[3][lane]));
+      float m = valid ? rmx : 0.f;
 #pragma unroll
-        for (int s = 16; s > 0; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
-        if (lane == 0) atomicMax(&P.ctl->maxrot_enc, enc_ord_d(m));
-      }
+      for (int s = 16; s > 0; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
+      if (lane == 0) atomicMax(&P.ctl->maxrot_enc, enc_ord_d(m));
     }
   }
 }
 
 template <bool INTEG>
 static cudaError_t launch_source_t(const Params& prm, const Ptrs& P, int compute_rot, cudaStream_t st) {
-  const int PW = prm.P / NWARP;
-  dim3 grid((prm.N + 31) / 32), block(128);
-  switch (PW) {
+  dim3 grid((prm.N + PTS - 1) / PTS), block(128);
+  switch (prm.P / 2) {
 #define CASE(X) \
   case X: k_source<X, INTEG><<<grid, block, 0, st>>>(prm, P, compute_rot); break;
-    CASE(2) CASE(3) CASE(4) CASE(6) CASE(8) CASE(9) CASE(12) CASE(16) CASE(18)
+    CASE(4) CASE(6) CASE(8) CASE(12) CASE(16) CASE(18) CASE(24)
 #undef CASE
     default: return cudaErrorInvalidConfiguration;
   }
@@ -241,9 +296,8 @@ cudaError_t launch_source_integ(const Params& prm, const Ptrs& P, cudaStream_t s
   return launch_source_t<true>(prm, P, 0, st);
 }
 bool supported_pm(int pm) {
-  int pw = pm / NWARP;
-  return pm % NWARP == 0 && (pw == 2 || pw == 3 || pw == 4 || pw == 6 || pw == 8 || pw == 9 || pw == 12 ||
-                             pw == 16 || pw == 18);
+  const int h = pm / 2;
+  return pm % 4 == 0 && (h == 4 || h == 6 || h == 8 || h == 12 || h == 16 || h == 18 || h == 24);
 }
 
 }  // namespace umwm

@@ -141,43 +141,24 @@ void collect_timings(Model& M) {
   M.evused = 0;
 }
 
-// per-(o,i) tables in device layout [o][t][ldN]; ghost column N
-std::vector<float> build_tables(const HostModel& H, int ldN) {
+// per-(o,i) tables in the blocked device layout [o][j/32][t][32]; ghost
+// point N holds the ghost values of cp0/cg0; points past N get finite
+// throw-away values (k = 1) so that idle lanes stay finite
+std::vector<float> build_tables(const HostModel& H, const Params& prm) {
   const int O = H.om, N = H.im;
-  std::vector<float> T((size_t)O * T_COUNT * ldN, 0.f);
-  auto put = [&](int t, const std::vector<float>& src, bool ghost) {
-    for (int o = 1; o <= O; ++o) {
-      float* row = &T[((size_t)(o - 1) * T_COUNT + t) * ldN];
-      for (int i = 1; i <= N; ++i) row[i - 1] = src[H.oi(o, i)];
-      if (ghost) row[N] = src[H.oi(o, 0)];
-    }
-  };
-  put(T_K, H.k, false);
-  put(T_CP0, H.cp0, true);
-  put(T_CG0, H.cg0, true);
-  put(T_LOGL2Z, H.logl2overz, false);
-  put(T_FKOVG, H.fkovg, false);
-  put(T_K4, H.k4, false);
-  put(T_K3DK, H.k3dk, false);
-  put(T_KDK, H.kdk, false);
-  put(T_COTHKD, H.cothkd, false);
-  put(T_SBF, H.sbf, false);
-  put(T_SDV, H.sdv, false);
-  put(T_BF1R, H.bf1r, false);
-  put(T_BF2R, H.bf2r, false);
-  // padding columns past N: keep the ghost values of cp0/cg0 and k=1 so that
-  // lanes beyond N compute finite throw-away values
-  for (int o = 0; o < O; ++o)
-    for (int j = N + 1; j < ldN; ++j) {
-      T[((size_t)o * T_COUNT + T_CP0) * ldN + j] = T[((size_t)o * T_COUNT + T_CP0) * ldN + N];
-      T[((size_t)o * T_COUNT + T_CG0) * ldN + j] = T[((size_t)o * T_COUNT + T_CG0) * ldN + N];
-    }
-  for (int o = 0; o < O; ++o)
-    for (int j = N; j < ldN; ++j) {
-      T[((size_t)o * T_COUNT + T_K) * ldN + j] = 1.f;
-      T[((size_t)o * T_COUNT + T_K4) * ldN + j] = 1.f;
-      T[((size_t)o * T_COUNT + T_KDK) * ldN + j] = 1.f;
-      T[((size_t)o * T_COUNT + T_COTHKD) * ldN + j] = 1.f;
+  std::vector<float> T((size_t)O * prm.NB * T_COUNT * 32, 0.f);
+  const std::vector<float>* src[T_COUNT] = {&H.k, &H.cp0, &H.cg0, &H.logl2overz, &H.fkovg, &H.k4, &H.k3dk,
+                                            &H.kdk, &H.cothkd, &H.sbf, &H.sdv, &H.bf1r, &H.bf2r};
+  for (int o = 1; o <= O; ++o)
+    for (int t = 0; t < T_COUNT; ++t) {
+      const bool ghost = (t == T_CP0 || t == T_CG0);
+      for (int j = 0; j < prm.ldN; ++j) {
+        float v;
+        if (j < N) v = (*src[t])[H.oi(o, j + 1)];
+        else if (ghost) v = (*src[t])[H.oi(o, 0)];
+        else v = (t == T_K || t == T_K4 || t == T_KDK || t == T_COTHKD) ? 1.f : 0.f;
+        T[tidx(prm, o - 1, t, j)] = v;
+      }
     }
   return T;
 }
@@ -259,7 +240,8 @@ int setup_params(Model& M) {
   if (H.gustiness > 0) return fail(UMWM_ERR_UNSUPPORTED, "gustiness > 0 (Fortran random_number) is not supported");
   Params& p = M.prm;
   p.N = H.im;
-  p.ldN = ((H.im + 1) + 31) / 32 * 32;
+  p.NB = (H.im + 1 + 31) / 32;
+  p.ldN = p.NB * 32;
   p.O = H.om; p.P = H.pm; p.NM = H.imm; p.mm = H.mm; p.nm = H.nm; p.lm = H.lm;
   p.iip = (H.iip >= 1 && H.iip <= H.im) ? H.iip - 1 : -1;
   p.g = H.g; p.explim = H.explim; p.sin_fac = H.sin_fac; p.fieldscale1 = H.fieldscale1;
@@ -303,7 +285,7 @@ int init_device(Model& M) {
   CU(D.alloc(&M.TAB, (size_t)p.O * T_COUNT * ldN, false));
   P.TAB = M.TAB;
   {
-    std::vector<float> T = build_tables(H, ldN);
+    std::vector<float> T = build_tables(H, p);
     CU(cudaMemcpy(M.TAB, T.data(), T.size() * 4, cudaMemcpyHostToDevice));
   }
   // wet-point integer arrays
