@@ -26,6 +26,11 @@ namespace umwm {
 
 constexpr int PTS_A = 64;  // wet points per CTA (4 warps x 16)
 
+// bulk prefetch of a contiguous, 16-byte aligned range into L2
+__device__ __forceinline__ void bulk_prefetch(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // stress_tail, umwm_stress.F90:300-311
 __device__ __forceinline__ float stress_tail(float w, float kmax) {
   const float kcap = 1e3f, a = 0.000112f, b = -0.01451f, c = -1.0186f;
@@ -117,8 +122,19 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
   const float dtaq = 0.25f * dta * oneovar;
 
   float sx = 0.f, sy = 0.f, dsx = 0.f, dsy = 0.f, txom = 0.f, tyom = 0.f;
+  // E* and ef of this block two frequencies ahead go to L2 in the background
+  const size_t blk = sidx(prm, 0, 0, jj & ~31);
+  auto pf = [&](int o) {
+    if (o < O && lane == 0) {
+      bulk_prefetch(P.ES + blk + (size_t)o * lstride, (unsigned)(prm.P * 128));
+      bulk_prefetch(P.EF + blk + (size_t)o * lstride, (unsigned)(prm.P * 128));
+    }
+  };
+  pf(0);
+  pf(1);
 
   for (int o = 0; o < O; ++o) {
+    pf(o + 2);
     const float* T = P.TAB + (size_t)o * tstride;
     const float* ESo = P.ES + (size_t)o * lstride;
     const float* EFo = P.EF + (size_t)o * lstride;

@@ -139,17 +139,14 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
 
   float A = 0.f, B = 0.f, C = 0.f;  // dummy coefficients of the current level
   float mx = 0.f, rmx = 0.f;
-  // three rotating buffers: level o lives in buffer o % 3
-  float eX[H], eY[H], eZ[H], sX[H], sY[H], sZ[H];
+  // the current level and the two previous ones (e and raw Sds per direction)
+  float ec[H], sc[H], e1[H], s1[H], e2[H], s2[H];
 #pragma unroll
-  for (int k = 0; k < H; ++k) { eX[k] = eY[k] = eZ[k] = sX[k] = sY[k] = sZ[k] = 0.f; }
-  Coef CX{}, CY{}, CZ{};
+  for (int k = 0; k < H; ++k) { ec[k] = sc[k] = e1[k] = s1[k] = e2[k] = s2[k] = 0.f; }
+  Coef Cc{}, C1{}, C2{};
 
-  // one frequency level o: load and Sds of level o into (ec, sc, Lc); in
-  // MODE_INTEG finish level o-2 whose values are in (e2, s2, L2), with the
-  // Snl partners at o-1 in (e1, s1)
-  auto step = [&](int o, float (&ec)[H], float (&sc)[H], Coef& Cc, const float (&e1)[H], const float (&s1)[H],
-                  const float (&e2)[H], const float (&s2)[H], const Coef& C2) {
+  const int OL = INTEG ? O + 2 : O;
+  for (int o = 0; o < OL; ++o) {
     pf(o + 2);
     if (o < O) {
       const float* r = Eb + (size_t)o * lstride;
@@ -250,13 +247,13 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
         }
       }
     }
-  };
 
-  const int OL = INTEG ? O + 2 : O;
-  for (int o = 0; o < OL; o += 3) {
-    step(o, eX, sX, CX, eZ, sZ, eY, sY, CY);
-    if (o + 1 < OL) step(o + 1, eY, sY, CY, eX, sX, eZ, sZ, CZ);
-    if (o + 2 < OL) step(o + 2, eZ, sZ, CZ, eY, sY, eX, sX, CX);
+    if (INTEG) {
+#pragma unroll
+      for (int k = 0; k < H; ++k) { e2[k] = e1[k]; s2[k] = s1[k]; e1[k] = ec[k]; s1[k] = sc[k]; }
+      C2 = C1;
+      C1 = Cc;
+    }
   }
 
   if (!INTEG) {
