@@ -95,6 +95,21 @@ int umwm_gpu_get_state(float* F, float* ust);
  * assignment, umwm_restart.F90:46-49).  Either pointer may be NULL. */
 int umwm_gpu_set_state(const float* F, const float* ust);
 
+/* Same output as umwm_gpu_get_state, for callers that cannot allocate device
+ * memory: a coupler checkpointing while a CUDA stream capture is active, a
+ * job whose GPU memory is fully committed, or a loop that must not pay
+ * cudaFree's device-wide synchronisation.  umwm_gpu_get_state allocates a
+ * temporary device buffer as large as the spectrum (om*pm*im floats); this
+ * variant allocates nothing and streams the spectrum to F through a fixed
+ * 16 MiB scratch array compiled into the library (held on every GPU that
+ * loads the library until the process exits), in chunks of whole wet points.
+ * A point's spectrum larger than the scratch (om*pm > 4 Mi floats) is rejected
+ * with UMWM_ERR_ARG.  The first call on a device looks up the scratch address
+ * there; make it before any stream capture.  All calls share the scratch:
+ * calls that overlap on the GPU race.  This entry point has no counterpart in
+ * the reference. */
+int umwm_gpu_get_state_noalloc(float* F, float* ust);
+
 /* Copy a named field into out (n floats).  Names are the reference's
  * variable names: wet-point fields (ht, mwp, mwd, mss, mwl, dwd, dwl, dwp,
  * dcp0, dcp, dcg0, dcg, momx, momy, cgmxx, cgmxy, cgmyy, ustar, cd, taux,

@@ -538,6 +538,80 @@ Model* need_model(bool device) {
   return g_model.get();
 }
 
+// ---------------------------------------------------------------------------
+// umwm_gpu_get_state_noalloc: the state read-back without device allocation.
+//
+// umwm_gpu_get_state transposes the spectrum into a temporary device buffer as
+// large as the spectrum itself (om*pm*im floats, 4.2 GB on a 1000x1000 grid),
+// allocated and freed on every call.  Some callers cannot do that: a coupler
+// that checkpoints the waves while a CUDA stream capture is active on the
+// device (allocation is not allowed during a global-mode capture), a job whose
+// GPU memory is fully committed to an ensemble or to another model's pool
+// allocator, or a time-critical loop that must not pay cudaFree's implicit
+// device-wide synchronisation.  This variant streams the transpose through a
+// fixed scratch area compiled into the library instead.
+//
+// The scratch is a file-scope __device__ array of NOALLOC_SCRATCH_FLOATS
+// floats (16 MiB).  Every GPU that loads the library holds it until the
+// process exits.  The spectrum goes through it in chunks of whole wet points
+// (NOALLOC_SCRATCH_FLOATS / (om*pm) points per chunk, 3149 for om=37, pm=36),
+// one transpose launch and one device-to-host copy per chunk.  A single
+// point's spectrum larger than the scratch is rejected with UMWM_ERR_ARG.
+//
+// Every call shares the one array and leaves the last chunk in it.  Each chunk
+// is written entirely before it is copied out, so nothing has to start at
+// zero.  Calls that overlap on the GPU (two host threads, or a call racing a
+// kernel launched by another thread on the same device) race on the scratch.
+// ---------------------------------------------------------------------------
+constexpr size_t NOALLOC_SCRATCH_FLOATS = (size_t)4 << 20;
+static __device__ __align__(256) float g_noalloc_scratch[NOALLOC_SCRATCH_FLOATS];
+
+// per-device address of the scratch array, looked up once per device
+struct NoallocSlot {
+  int device;
+  float* ptr;
+};
+std::vector<NoallocSlot> g_noalloc_slots;
+
+int noalloc_scratch(float** out) {
+  int dev = 0;
+  CU(cudaGetDevice(&dev));
+  for (const auto& s : g_noalloc_slots)
+    if (s.device == dev) {
+      *out = s.ptr;
+      return UMWM_OK;
+    }
+  // first call on this device: resolve the array's device address with this
+  // device current (the host-side symbol is only a stand-in, not a device
+  // address)
+  float* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return fail(UMWM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  g_noalloc_slots.push_back({dev, p});
+  *out = p;
+  return UMWM_OK;
+}
+
+// transpose of wet points [j0, j0+nj) into the reference order F(om,pm,.)
+__global__ void k_to_ref_chunk(const Params prm, const float* __restrict__ E, float* __restrict__ F, int j0, int nj) {
+  __shared__ float tile[32][33];
+  const int R = prm.O * prm.P;
+  const int c0 = blockIdx.x * 32, jb = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  for (int k = ty; k < 32; k += blockDim.y) {
+    const int c = c0 + k;
+    if (c < R && jb + tx < nj) {
+      const int o = c % prm.O, p = c / prm.O;
+      tile[k][tx] = E[sidx(prm, o, p, j0 + jb + tx)];
+    }
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += blockDim.y) {
+    const int jrow = jb + k, c = c0 + tx;
+    if (jrow < nj && c < R) F[(size_t)jrow * R + c] = tile[tx][k];
+  }
+}
+
 }  // namespace
 }  // namespace umwm
 
@@ -656,6 +730,36 @@ int umwm_gpu_get_state(float* F, float* ust) {
     if (e == cudaSuccess) e = cudaMemcpy(F, tmp, n * 4, cudaMemcpyDeviceToHost);
     cudaFree(tmp);
     CU(e);
+  }
+  if (ust) CU(cudaMemcpy(ust, M->P.ustar, (size_t)p.N * 4, cudaMemcpyDeviceToHost));
+  return UMWM_OK;
+}
+
+// See the note at g_noalloc_scratch: the state read-back without any device
+// allocation, through the library's fixed scratch area.  The first call on a
+// device looks up the scratch address on that device (cudaGetSymbolAddress),
+// so make the first call before any stream capture begins.
+int umwm_gpu_get_state_noalloc(float* F, float* ust) {
+  Model* M = need_model(true);
+  if (!M) return UMWM_ERR_STATE;
+  const Params& p = M->prm;
+  const size_t R = (size_t)p.O * p.P;
+  if (R > NOALLOC_SCRATCH_FLOATS)
+    return fail(UMWM_ERR_ARG, "get_state_noalloc: one point's spectrum (om*pm floats) exceeds the 16 MiB scratch");
+  float* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  CU(cudaStreamSynchronize(M->st));
+  if (F) {
+    const int chunk = (int)(NOALLOC_SCRATCH_FLOATS / R);
+    for (int j0 = 0; j0 < p.N; j0 += chunk) {
+      const int nj = std::min(chunk, p.N - j0);
+      dim3 grid((unsigned)((R + 31) / 32), (unsigned)((nj + 31) / 32)), block(32, 8);
+      k_to_ref_chunk<<<grid, block, 0, M->st>>>(p, M->E, scratch, j0, nj);
+      CU(cudaGetLastError());
+      CU(cudaMemcpyAsync(F + (size_t)j0 * R, scratch, (size_t)nj * R * sizeof(float), cudaMemcpyDeviceToHost, M->st));
+      CU(cudaStreamSynchronize(M->st));
+    }
   }
   if (ust) CU(cudaMemcpy(ust, M->P.ustar, (size_t)p.N * 4, cudaMemcpyDeviceToHost));
   return UMWM_OK;

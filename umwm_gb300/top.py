@@ -170,6 +170,16 @@ def get_state():
     return F, u
 
 
+def get_state_noalloc():
+    """get_state without device allocation: the spectrum goes to the host
+    through the library's fixed 16 MiB scratch (see umwm_gpu_get_state_noalloc)."""
+    d = dims()
+    F = np.zeros((d["im"], d["pm"], d["om"]), dtype=np.float32)
+    u = np.zeros(d["im"], dtype=np.float32)
+    check(lib().umwm_gpu_get_state_noalloc(F.ctypes.data_as(_fp), u.ctypes.data_as(_fp)))
+    return F, u
+
+
 def set_state(F=None, ust=None):
     Fp = _f32(F).ravel() if F is not None else None
     up = _f32(ust).ravel() if ust is not None else None
