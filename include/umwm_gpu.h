@@ -82,6 +82,26 @@ int umwm_gpu_finalize(void);
  * the unrolled grid and tables can be inspected with the getters below. */
 int umwm_gpu_setup_host(const char* nml_text);
 
+/* ---- ensembles: many domains advanced together ---------------------------
+ * An ensemble is one model over several domains ("members") that share the
+ * spectral grid, physics, forcing switches, dtg and start time; each has its
+ * own grid, depth, forcing, restart and dynamic time step.  Kernels run over
+ * the concatenated wet points of all members, one launch per stage per
+ * substep for the whole ensemble; a member that has reached the end of the
+ * current dtg sits out the remaining substeps of that dtg.  Each member runs
+ * exactly the computation it runs alone (no extension of the reference; it
+ * replaces running the reference once per member). */
+
+/* Add a member: its namelist text, and the inputs staged so far with the
+ * put_* calls (the staging is then cleared for the next member). */
+int umwm_gpu_ensemble_add(const char* nml_text);
+
+/* Initialize every added member as one model (umwm_initialize for each). */
+int umwm_gpu_ensemble_initialize(void);
+
+/* Select the member the state and field getters/setters act on (default 0). */
+int umwm_gpu_select_member(int member);
+
 /* ---- state and fields ---------------------------------------------------- */
 
 /* dims[0..7] = mm, nm, om, pm, im, imm, lm, substeps-so-far */

@@ -5,6 +5,6 @@ this package is its Python binding, a mirror of the reference's umwm_top
 module, and the synthetic-workload generators.
 """
 from ._lib import EXPORTS, LIB_PATH, UmwmError, lib  # noqa: F401
-from .top import (clear_inputs, dims, get_field, get_field_i, get_screen, get_state, get_state_noalloc, put_exclude,  # noqa: F401
-                  put_forcing, put_gridtopo, put_restart, set_option, set_state, setup_host, stat,
-                  umwm_finalize, umwm_initialize, umwm_run)
+from .top import (clear_inputs, dims, ensemble_add, ensemble_initialize, get_field, get_field_i,  # noqa: F401
+                  get_screen, get_state, get_state_noalloc, put_exclude, put_forcing, put_gridtopo, put_restart,
+                  select_member, set_option, set_state, setup_host, stat, umwm_finalize, umwm_initialize, umwm_run)

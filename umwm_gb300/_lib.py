@@ -16,7 +16,8 @@ EXPORTS = [
     "umwm_gpu_finalize", "umwm_gpu_setup_host", "umwm_gpu_get_dims", "umwm_gpu_get_state", "umwm_gpu_set_state",
     "umwm_gpu_get_state_noalloc",
     "umwm_gpu_get_field", "umwm_gpu_get_field_i", "umwm_gpu_get_screen", "umwm_gpu_set_option",
-    "umwm_gpu_get_stat", "umwm_gpu_last_error",
+    "umwm_gpu_get_stat", "umwm_gpu_last_error", "umwm_gpu_ensemble_add", "umwm_gpu_ensemble_initialize",
+    "umwm_gpu_select_member",
 ]
 
 ERRORS = {0: "UMWM_OK", 1: "UMWM_ERR_NAMELIST", 2: "UMWM_ERR_INPUT", 3: "UMWM_ERR_CUDA", 4: "UMWM_ERR_NONFINITE",
@@ -64,6 +65,9 @@ def lib():
         "umwm_gpu_get_field_i": [c, ip, ctypes.c_long],
         "umwm_gpu_get_screen": [dp, ctypes.c_long, ctypes.POINTER(ctypes.c_long)],
         "umwm_gpu_set_option": [c, ctypes.c_double],
+        "umwm_gpu_ensemble_add": [c],
+        "umwm_gpu_ensemble_initialize": [],
+        "umwm_gpu_select_member": [ctypes.c_int],
     }
     for name, args in sig.items():
         f = getattr(L, name)

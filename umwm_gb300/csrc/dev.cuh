@@ -1,8 +1,11 @@
 // Device-side definitions shared by the GB300 UMWM kernels.
 //
-// HBM layout.  N wet points plus a ghost point at index N (the reference's
-// aliased land neighbour iistart-1), grouped in NB = ceil((N+1)/32) blocks
-// of 32 consecutive wet points (ldN = 32 NB):
+// One model is an ensemble of members (a single domain is a one-member
+// ensemble).  Member m owns the wet indices [off, off + N) of a common index
+// space, then its own ghost point at off + N (the reference's aliased land
+// neighbour iistart-1), padded to a multiple of 64 points so that every CTA
+// tile belongs to one member.  The index space is grouped in NB blocks of 32
+// consecutive points (ldN = 32 NB):
 //   spectrum arrays E, ES (= E* after the source half-step), EF:
 //       [o][j/32][p][32]: one frequency of one 32-point block is a
 //       contiguous P*128-byte region; within it direction p is a 128-byte
@@ -38,11 +41,19 @@ enum TableRow {
   T_COUNT
 };
 
+constexpr int TILE = 64;  // wet points per CTA tile of the spectral kernels
+
+struct Ctl;
+struct Member;
+
 struct Params {
-  int N, ldN, NB, O, P, NM, mm, nm, lm;
-  int iip;  // 0-based wet index of the screen point, -1 if none
+  int Ntot, ldN, NB, O, P, NMtot, lm;
+  int nmem;              // members
+  int ntiles;            // CTA tiles of TILE points over the whole index space
+  const Member* mem;     // [nmem]
+  const int* tile_mem;   // member of each tile [ntiles]
   float g, explim, sin_fac, fieldscale1, fieldscale2, twopisds_fac, sds_power, inv_sds_power, mss_fac, snl_fac,
-      sdt_fac, z, nu_air, kappa, fprog, dth, dthg, oneovdth, dtamin, dtg, fice_lth, fice_uth, eulerinv, rhow0;
+      sdt_fac, z, nu_air, kappa, fprog, dth, dthg, oneovdth, dtg, fice_lth, fice_uth, eulerinv, rhow0;
   int winds, currents, air_density, water_density, seaice, restart, curvilinear, isglobal;
   int ice_possible;  // fice can exceed fice_lth somewhere
   float f[MAX_OM], dom[MAX_OM];
@@ -50,7 +61,7 @@ struct Params {
   float depth[MAX_LM];
 };
 
-// Device-resident control block of the inner (dynamic-dts) loop.
+// Device-resident control block of the inner (dynamic-dts) loop, one per member.
 struct Ctl {
   float sumt, dts, dta, dtr, dtr_temp;
   unsigned minphys_enc;   // ordered encoding of min_i(explim/max|arg|)
@@ -59,18 +70,38 @@ struct Ctl {
   int zerocurrents;       // latched for propagation of this substep
   int first;              // reference's 'first' (first substep of the first run)
   int compute_rot;        // rotation recomputed this substep
-  int done;               // sumt >= dtg after this substep
+  int done;               // sumt >= dtg: the member has finished the current dtg
+  int running;            // the member takes part in the current substep
   int substep;            // substeps since initialize
   int err;                // error flags (bit 0: timeout)
   int log_count;
 };
 
+// Per-member ranges, scalars and pointers.
+struct Member {
+  int off, N, ghost;       // wet indices [off, off+N), ghost point off+N
+  int nmoff, NM, mm, nm;   // all-point range [nmoff, nmoff+NM) and 2-d grid
+  int iip;                 // index of the screen point, -1 if none
+  float dtamin;
+  Ctl* ctl;
+  double* log;             // screen lines, 8 per substep
+  int log_cap;
+  const int *mi, *ni;      // 1-based (m, n) of each all-point index (member-local, [NM])
+  // forcing levels (mm*nm, Fortran order): b = n, f = n+1
+  const float *uwb, *uwf, *vwb, *vwf, *ucb, *ucf, *vcb, *vcf, *rhoab, *rhoaf, *rhowb, *rhowf, *ficeb, *ficef;
+};
+
+// control shared by all members (one per model)
+struct Global {
+  int not_done;            // members still inside the current dtg after this substep
+};
+
 struct Ptrs {
-  float *E, *ES, *EF;  // spectrum arrays [O][P][ldN]
+  float *E, *ES, *EF;  // spectrum arrays (EF aliases E: each bin is read and then overwritten by one thread)
   const float* TAB;     // [O][T_COUNT][ldN]
   // wet-point arrays [ldN]
-  const int *ie, *iw, *in, *is;      // aliased neighbours (N = ghost)
-  const int *iie, *iiw, *iin, *iis;  // true neighbours, 0-based over imm
+  const int *ie, *iw, *in, *is;      // aliased neighbours (global index; the member's ghost for land)
+  const int *iie, *iiw, *iin, *iis;  // true neighbours (global all-point index)
   const float *oneovar, *oneovdx, *oneovdy, *dxn, *dxs, *dye, *dyw, *d, *curv;
   int* oc;
   int* oc_rot;      // oc at the last rotation computation
@@ -82,19 +113,15 @@ struct Ptrs {
   float* fcutoff;
   float* phys;      // physics_time_step
   float* sice_v;    // per-point sea-ice attenuation factor (0 when no ice)
-  // all-point arrays [NM] (0-based unrolled index, land included)
+  // all-point arrays, member m at [nmoff, nmoff+NM) (land included; wet
+  // points first, in the member's unrolled order)
   float *wspd, *wdir, *uc, *vc, *rhoa, *rhow, *rhorat, *fice;
-  const int *mi, *ni;  // 1-based (m, n) of each unrolled index
-  // forcing levels (mm*nm, Fortran order): b = n, f = n+1
-  const float *uwb, *uwf, *vwb, *vwf, *ucb, *ucf, *vcb, *vcf, *rhoab, *rhoaf, *rhowb, *rhowf, *ficeb, *ficef;
   // Stokes drift [lm][ldN] and e-folding depth
   float *us, *vs, *ds;
   // diagnostics [ldN]
   float *ht, *mwp, *mwd, *mss, *mwl, *dwd, *dwl, *dwp, *dcp0, *dcp, *dcg0, *dcg, *momx, *momy, *cgmxx, *cgmxy,
       *cgmyy;
-  Ctl* ctl;
-  double* log;  // screen lines, 8 per substep
-  int log_cap;
+  Global* glob;
 };
 
 // element offsets in the blocked layouts

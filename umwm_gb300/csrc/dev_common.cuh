@@ -39,18 +39,22 @@ struct WindIn {
   int oc;  // 1-based cut-off index; 0-based level o is prognostic when o < oc
 };
 
-__device__ __forceinline__ WindIn load_wind(const Params& prm, const Ptrs& P, int jj, float ustar) {
+// jj: global wet index; ja: its all-point index
+__device__ __forceinline__ WindIn load_wind(const Params& prm, const Ptrs& P, int jj, int ja, float ustar) {
   WindIn w;
-  w.wspd = P.wspd[jj];
-  w.uc = P.uc[jj];
-  w.vc = P.vc[jj];
+  w.wspd = P.wspd[ja];
+  w.uc = P.uc[ja];
+  w.vc = P.vc[ja];
   w.ustar25 = 2.5f * ustar;
   w.shelt_sf = P.shelt[jj] / prm.sin_fac;
   // (1 - fice) * twopi * rhorat
-  w.c1 = ((1.f - P.fice[jj]) * (2.f * 3.14159274f)) * P.rhorat[jj];
+  w.c1 = ((1.f - P.fice[ja]) * (2.f * 3.14159274f)) * P.rhorat[ja];
   w.oc = P.oc[jj];
   return w;
 }
+
+// all-point index of a wet (or ghost) point of member M
+__device__ __forceinline__ int apt(const Member& M, int j) { return M.nmoff + (j - M.off); }
 
 // Sin at (o, p) given cw = cos(wdir - th(p)) and the level tables.
 __device__ __forceinline__ float sin_bin(const Params& prm, const WindIn& w, float cw, float cth, float sth,

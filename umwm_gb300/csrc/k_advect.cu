@@ -24,7 +24,7 @@
 
 namespace umwm {
 
-constexpr int PTS_A = 64;  // wet points per CTA (4 warps x 16)
+constexpr int PTS_A = TILE;  // wet points per CTA (4 warps x 16)
 
 // bulk prefetch of a contiguous, 16-byte aligned range into L2
 __device__ __forceinline__ void bulk_prefetch(const void* p, unsigned bytes) {
@@ -58,31 +58,35 @@ template <int H, bool CURV>
 __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs P) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int j16 = lane & 15, half = lane >> 4;
-  const int N = prm.N, O = prm.O;
+  const int O = prm.O;
+  const Member& Mb = prm.mem[prm.tile_mem[blockIdx.x]];
+  const Ctl* ctl = Mb.ctl;
+  if (!ctl->running) return;  // the member has finished the current dtg
+  const int N = Mb.ghost;
   const int j = blockIdx.x * PTS_A + w * 16 + j16;
   const bool valid = j < N;
   const int jj = valid ? j : N;
+  const int ja = apt(Mb, jj);
   const float sg = half ? -1.f : 1.f;
   __shared__ float cws[H][128];
   __shared__ float ccs[CURV ? H : 1][128], scs[CURV ? H : 1][128];
 
-  const Ctl* ctl = P.ctl;
   const float dta = ctl->dta, dtr = ctl->dtr;
   const bool zerocur = ctl->zerocurrents != 0;
 
   const int ie = P.ie[jj], iw = P.iw[jj], in = P.in[jj], is = P.is[jj];
   const int oc = P.oc[jj], ocr = P.oc_rot[jj];
-  const bool ice = P.fice[jj] > prm.fice_uth;
+  const bool ice = P.fice[ja] > prm.fice_uth;
   const float oneovar = P.oneovar[jj], dxn = P.dxn[jj], dxs = P.dxs[jj], dye = P.dye[jj], dyw = P.dyw[jj];
   const float odx = P.oneovdx[jj], ody = P.oneovdy[jj];
   const float ustar = P.ustar[jj];
-  const WindIn wi = load_wind(prm, P, jj, ustar);
-  const float wdir = P.wdir[jj];
+  const WindIn wi = load_wind(prm, P, jj, ja, ustar);
+  const float wdir = P.wdir[ja];
   const float ucg = sg * wi.uc, vcg = sg * wi.vc;
 
   // current advection, umwm_advection.F90:62-82, folded per point
   float F0 = 0.f, fedn = 0.f, fwup = 0.f, fndn = 0.f, fsup = 0.f;
-  const float uci = P.uc[jj], vci = P.vc[jj];
+  const float uci = P.uc[ja], vci = P.vc[ja];
   const float ucn = P.uc[P.iin[jj]], ucs = P.uc[P.iis[jj]];
   const float vce = P.vc[P.iie[jj]], vcw = P.vc[P.iiw[jj]];
   if (!zerocur) {
@@ -115,8 +119,8 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
                oN = sidx(prm, 0, 0, in) + hoff, oSs = sidx(prm, 0, 0, is) + hoff;
   // stress_vector_integral divides by cp0 of the previous unrolled point
   // (assumed-shape dummy with lower bound 1 over cp0(:,0:im)),
-  // umwm_stress.F90:401, :495-513
-  const int jprev = (jj == 0 || jj >= N) ? N : jj - 1;
+  // umwm_stress.F90:401, :495-513; the member's first point uses its ghost
+  const int jprev = (jj == Mb.off || jj >= N) ? N : jj - 1;
   const size_t tS = tidx(prm, 0, 0, jj), tE = tidx(prm, 0, 0, ie), tW = tidx(prm, 0, 0, iw),
                tN = tidx(prm, 0, 0, in), tSs = tidx(prm, 0, 0, is), tP = tidx(prm, 0, 0, jprev);
   const float dtaq = 0.25f * dta * oneovar;
@@ -141,7 +145,7 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
     float* Eo = P.E + (size_t)o * lstride;
     float ef[H];
 #pragma unroll
-    for (int k = 0; k < H; ++k) ef[k] = __ldg(EFo + oS + k * 32);
+    for (int k = 0; k < H; ++k) ef[k] = EFo[oS + k * 32];  // EF aliases E, written below
     const bool prog = o < oc;
     const unsigned pm = __ballot_sync(0xffffffffu, prog);
     if (prog) {
@@ -224,7 +228,7 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
   tyom += __shfl_xor_sync(0xffffffffu, tyom, 16);
   if (half != 0 || !valid) return;
   // ---- stress('atm') per point, umwm_stress.F90:216-262
-  const float rhow = P.rhow[j], rhoa = P.rhoa[j], wspd = wi.wspd;
+  const float rhow = P.rhow[ja], rhoa = P.rhoa[ja], wspd = wi.wspd;
   const float kom = __ldg(P.TAB + (size_t)(O - 1) * tstride + tS + T_K * 32);
   const float tl = stress_tail(wspd, kom);
   const float tax = txom * kom * tl * rhow * prm.dthg;
@@ -260,7 +264,7 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
 }
 
 cudaError_t launch_advect(const Params& prm, const Ptrs& P, cudaStream_t st) {
-  dim3 grid((prm.N + PTS_A - 1) / PTS_A), block(128);
+  dim3 grid(prm.ntiles), block(128);
   const bool curv = prm.curvilinear != 0;
   switch (prm.P / 2) {
 #define CASE(X)                                                          \

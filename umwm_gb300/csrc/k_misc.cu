@@ -15,39 +15,44 @@ namespace umwm {
 // clamp wspd, rhorat; per wet point the cut-off index oc and the
 // sheltering coefficient (umwm_source_functions.F90:52).
 __global__ void k_prep(const Params prm, const Ptrs P, int compute_rot) {
-  const float sumt = P.ctl->sumt, dtg = prm.dtg;
+  const Member& M = prm.mem[blockIdx.y];
+  Ctl* ctl = M.ctl;
+  if (ctl->done) return;
+  const float sumt = ctl->sumt, dtg = prm.dtg;
   const float a = 1.f - sumt / dtg;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < prm.NM; i += gridDim.x * blockDim.x) {
-    const int q = (P.mi[i] - 1) + (P.ni[i] - 1) * prm.mm;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.NM; i += gridDim.x * blockDim.x) {
+    const int q = (M.mi[i] - 1) + (M.ni[i] - 1) * M.mm;
+    const int ia = M.nmoff + i;
     if (prm.winds) {
-      float uw = P.uwb[q] * a + P.uwf[q] * sumt / dtg;
-      float vw = P.vwb[q] * a + P.vwf[q] * sumt / dtg;
-      P.wspd[i] = sqrtf(uw * uw + vw * vw);
-      P.wdir[i] = atan2f(vw, uw);
+      float uw = M.uwb[q] * a + M.uwf[q] * sumt / dtg;
+      float vw = M.vwb[q] * a + M.vwf[q] * sumt / dtg;
+      P.wspd[ia] = sqrtf(uw * uw + vw * vw);
+      P.wdir[ia] = atan2f(vw, uw);
     }
-    if (prm.seaice) P.fice[i] = P.ficeb[q] * a + P.ficef[q] * sumt / dtg;
+    if (prm.seaice) P.fice[ia] = M.ficeb[q] * a + M.ficef[q] * sumt / dtg;
     if (prm.currents) {
-      P.uc[i] = P.ucb[q] * a + P.ucf[q] * sumt / dtg;
-      P.vc[i] = P.vcb[q] * a + P.vcf[q] * sumt / dtg;
+      P.uc[ia] = M.ucb[q] * a + M.ucf[q] * sumt / dtg;
+      P.vc[ia] = M.vcb[q] * a + M.vcf[q] * sumt / dtg;
     }
-    if (prm.air_density) P.rhoa[i] = P.rhoab[q] * a + P.rhoaf[q] * sumt / dtg;
-    if (prm.water_density) P.rhow[i] = P.rhowb[q] * a + P.rhowf[q] * sumt / dtg;
-    P.rhorat[i] = P.rhoa[i] / P.rhow[i];
-    const float ws = fmaxf(P.wspd[i], 1e-2f);
-    P.wspd[i] = ws;
-    if ((prm.isglobal || i < prm.N) && (P.uc[i] != 0.f || P.vc[i] != 0.f)) P.ctl->anycurrent = 1;
-    if (i < prm.N) {
+    if (prm.air_density) P.rhoa[ia] = M.rhoab[q] * a + M.rhoaf[q] * sumt / dtg;
+    if (prm.water_density) P.rhow[ia] = M.rhowb[q] * a + M.rhowf[q] * sumt / dtg;
+    P.rhorat[ia] = P.rhoa[ia] / P.rhow[ia];
+    const float ws = fmaxf(P.wspd[ia], 1e-2f);
+    P.wspd[ia] = ws;
+    if ((prm.isglobal || i < M.N) && (P.uc[ia] != 0.f || P.vc[ia] != 0.f)) ctl->anycurrent = 1;
+    if (i < M.N) {
+      const int j = M.off + i;
       float fc = 0.53f * prm.g / ws;
       if (fc > prm.fprog) fc = prm.fprog;
-      P.fcutoff[i] = fc;
+      P.fcutoff[j] = fc;
       int oc = 1;
       for (int o = prm.O - 2; o >= 1; --o) {
         oc = o;
         if (fc > prm.f[o - 1]) break;
       }
-      P.oc[i] = oc;
-      if (compute_rot) P.oc_rot[i] = oc;
-      P.shelt[i] = shelter_coare35(ws);
+      P.oc[j] = oc;
+      if (compute_rot) P.oc_rot[j] = oc;
+      P.shelt[j] = shelter_coare35(ws);
     }
   }
 }
@@ -56,33 +61,47 @@ __global__ void k_prep(const Params prm, const Ptrs P, int compute_rot) {
 // first-step rule and sumt update (umwm_physics.F90:41-58); refraction's
 // dtr (umwm_advection.F90:145-158).  One thread.
 __global__ void k_dts(const Params prm, const Ptrs P, int compute_rot, int first) {
-  Ctl& c = *P.ctl;
-  float mn = dec_ord_d(c.minphys_enc);
-  float dts = fminf(fminf(mn, prm.dtamin), prm.dtg - c.sumt);
-  if (!prm.restart && first) dts = 0.f;
-  c.dts = dts;
-  c.dta = dts;
-  c.sumt = c.sumt + dts;
-  if (compute_rot) {
-    float mx = dec_ord_d(c.maxrot_enc);
-    c.dtr_temp = (mx <= FLT_MIN) ? dts : prm.dth / mx;
+  int left = 0;
+  for (int m = threadIdx.x; m < prm.nmem; m += blockDim.x) {
+    const Member& M = prm.mem[m];
+    Ctl& c = *M.ctl;
+    if (c.done) {  // finished this dtg in an earlier substep
+      c.running = 0;
+      continue;
+    }
+    float mn = dec_ord_d(c.minphys_enc);
+    float dts = fminf(fminf(mn, M.dtamin), prm.dtg - c.sumt);
+    if (!prm.restart && first) dts = 0.f;
+    c.dts = dts;
+    c.dta = dts;
+    c.sumt = c.sumt + dts;
+    if (compute_rot) {
+      float mx = dec_ord_d(c.maxrot_enc);
+      c.dtr_temp = (mx <= FLT_MIN) ? dts : prm.dth / mx;
+    }
+    c.dtr = fminf(c.dtr_temp, dts);
+    c.zerocurrents = c.anycurrent ? 0 : 1;
+    c.anycurrent = 0;
+    c.minphys_enc = enc_ord_d(__int_as_float(0x7f800000));
+    c.maxrot_enc = enc_ord_d(0.f);
+    c.done = (c.sumt < prm.dtg) ? 0 : 1;
+    c.running = 1;
+    c.first = first;
+    left += !c.done;
   }
-  c.dtr = fminf(c.dtr_temp, dts);
-  c.zerocurrents = c.anycurrent ? 0 : 1;
-  c.anycurrent = 0;
-  c.minphys_enc = enc_ord_d(__int_as_float(0x7f800000));
-  c.maxrot_enc = enc_ord_d(0.f);
-  c.done = (c.sumt < prm.dtg) ? 0 : 1;
-  c.first = first;
+  left = __syncthreads_count(left > 0) ? 1 : 0;  // any member left in this block
+  if (threadIdx.x == 0) P.glob->not_done = left;
 }
 
 // s_ice: significant wave height where fice > fice_lth and the attenuation
 // factor C1*Hs (Hs < 3 m) or C1*3 (umwm_source_functions.F90:108-153).
 __global__ void k_sice(const Params prm, const Ptrs P) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= prm.N) return;
+  if (j >= prm.Ntot) return;
+  const Member& M = prm.mem[prm.tile_mem[j / TILE]];
+  if (j >= M.ghost || M.ctl->done) return;
   float sv = 0.f;
-  if (P.fice[j] > prm.fice_lth) {
+  if (P.fice[apt(M, j)] > prm.fice_lth) {
     float h = 0.f;
     for (int p = 0; p < prm.P; ++p)
       for (int o = 0; o < prm.O; ++o)
@@ -97,7 +116,10 @@ __global__ void k_sice(const Params prm, const Ptrs P) {
 // diag, umwm_physics.F90:89-205 (one thread per wet point, reference loop order)
 __global__ void k_diag(const Params prm, const Ptrs P) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= prm.N) return;
+  if (j >= prm.Ntot) return;
+  const Member& Mb = prm.mem[prm.tile_mem[j / TILE]];
+  if (j >= Mb.ghost) return;
+  const int ja = apt(Mb, j);
   const int O = prm.O, NP = prm.P, oc = P.oc[j];
   const float* E = P.E;
   auto tab = [&](int t, int o) { return P.TAB[tidx(prm, o, t, j)]; };
@@ -125,7 +147,7 @@ __global__ void k_diag(const Params prm, const Ptrs P) {
     }
     xc += mag * cth; yc += mag * sth;
   }
-  const float rw = P.rhow[j] * prm.dthg;
+  const float rw = P.rhow[ja] * prm.dthg;
   P.mwp[j] = sqrtf(m0 / (m2 + FLT_MIN));
   P.momx[j] = mx * rw; P.momy[j] = my * rw;
   P.cgmxx[j] = cxx * rw; P.cgmxy[j] = cxy * rw; P.cgmyy[j] = cyy * rw;
@@ -138,7 +160,7 @@ __global__ void k_diag(const Params prm, const Ptrs P) {
   P.dwp[j] = 1.f / prm.f[op];
   const float c0 = tab(T_CP0, op), g0 = tab(T_CG0, op);
   P.dcp0[j] = c0; P.dcg0[j] = g0;
-  const float uc = P.uc[j], vc = P.vc[j];
+  const float uc = P.uc[ja], vc = P.vc[ja];
   P.dcp[j] = c0 + uc * prm.cth[pp] + vc * prm.sth[pp];
   P.dcg[j] = g0 + uc * prm.cth[pp] + vc * prm.sth[pp];
 }
@@ -147,7 +169,9 @@ __global__ void k_diag(const Params prm, const Ptrs P) {
 // instead of stored (it would be om*im*lm floats).
 __global__ void k_stokes(const Params prm, const Ptrs P) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= prm.N) return;
+  if (j >= prm.Ntot) return;
+  const Member& Mb = prm.mem[prm.tile_mem[j / TILE]];
+  if (j >= Mb.ghost) return;
   const int O = prm.O, NP = prm.P, ldN = prm.ldN;
   float X[MAX_OM], Y[MAX_OM];
   for (int o = 0; o < O; ++o) {
@@ -202,8 +226,10 @@ __global__ void k_stokes(const Params prm, const Ptrs P) {
 // also clears 'first' after the first substep.
 __global__ void k_screen(const Params prm, const Ptrs P) {
   __shared__ float s0[256], s2[256];
-  Ctl& c = *P.ctl;
-  const int j = prm.iip;
+  const Member& M = prm.mem[blockIdx.x];
+  Ctl& c = *M.ctl;
+  if (!c.running) return;
+  const int j = M.iip;
   float a = 0.f, b = 0.f;
   if (j >= 0) {
     for (int b_ = threadIdx.x; b_ < prm.O * prm.P; b_ += blockDim.x) {
@@ -222,12 +248,13 @@ __global__ void k_screen(const Params prm, const Ptrs P) {
   }
   if (threadIdx.x == 0) {
     const int r = c.log_count;
-    if (r < P.log_cap && j >= 0) {
-      double* L = P.log + (size_t)r * 8;
+    if (r < M.log_cap && j >= 0) {
+      double* L = M.log + (size_t)r * 8;
+      const int ja = apt(M, j);
       L[0] = c.sumt / prm.dtg;
       L[1] = c.dts;
-      L[2] = P.wspd[j];
-      L[3] = P.wdir[j];
+      L[2] = P.wspd[ja];
+      L[3] = P.wdir[ja];
       L[4] = 4.f * sqrtf(s0[0] * prm.dth);
       L[5] = sqrtf(s0[0] / s2[0]);
       L[6] = P.cd[j] * 1e3f;
@@ -240,41 +267,50 @@ __global__ void k_screen(const Params prm, const Ptrs P) {
 }
 
 // Reference order F(om,pm,im) (o fastest) <-> the blocked device layout.
-__global__ void k_to_ref(const Params prm, const float* __restrict__ E, float* __restrict__ F) {
+__global__ void k_to_ref(const Params prm, const float* __restrict__ E, float* __restrict__ F, int off, int n) {
   __shared__ float tile[32][33];
   const int R = prm.O * prm.P;
   const int c0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
   for (int k = ty; k < 32; k += blockDim.y) {
     const int c = c0 + k;  // column of F: c = p*O + o
-    if (c < R && j0 + tx < prm.N) {
+    if (c < R && j0 + tx < n) {
       const int o = c % prm.O, p = c / prm.O;
-      tile[k][tx] = E[sidx(prm, o, p, j0 + tx)];
+      tile[k][tx] = E[sidx(prm, o, p, off + j0 + tx)];
     }
   }
   __syncthreads();
   for (int k = ty; k < 32; k += blockDim.y) {
     const int jrow = j0 + k, c = c0 + tx;
-    if (jrow < prm.N && c < R) F[(size_t)jrow * R + c] = tile[tx][k];
+    if (jrow < n && c < R) F[(size_t)jrow * R + c] = tile[tx][k];
   }
 }
 
-__global__ void k_from_ref(const Params prm, const float* __restrict__ F, float* __restrict__ E) {
+__global__ void k_from_ref(const Params prm, const float* __restrict__ F, float* __restrict__ E, int off, int n) {
   __shared__ float tile[32][33];
   const int R = prm.O * prm.P;
   const int c0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
   for (int k = ty; k < 32; k += blockDim.y) {
     const int jrow = j0 + k, c = c0 + tx;
-    if (jrow < prm.N && c < R) tile[k][tx] = F[(size_t)jrow * R + c];
+    if (jrow < n && c < R) tile[k][tx] = F[(size_t)jrow * R + c];
   }
   __syncthreads();
   for (int k = ty; k < 32; k += blockDim.y) {
     const int c = c0 + k;
-    if (c < R && j0 + tx < prm.N) {
+    if (c < R && j0 + tx < n) {
       const int o = c % prm.O, p = c / prm.O;
-      E[sidx(prm, o, p, j0 + tx)] = tile[tx][k];
+      E[sidx(prm, o, p, off + j0 + tx)] = tile[tx][k];
     }
+  }
+}
+
+// start of a dtg: sumt = 0 and no member done (umwm_top.F90:88)
+__global__ void k_begin_dtg(const Params prm) {
+  for (int m = threadIdx.x; m < prm.nmem; m += blockDim.x) {
+    Ctl& c = *prm.mem[m].ctl;
+    c.sumt = 0.f;
+    c.done = 0;
   }
 }
 
@@ -288,38 +324,43 @@ static int grid_for(long n, int block) {
   return (int)(g < 1 ? 1 : g);
 }
 
-cudaError_t launch_prep(const Params& prm, const Ptrs& P, int compute_rot, cudaStream_t st) {
-  k_prep<<<grid_for(prm.NM, 256), 256, 0, st>>>(prm, P, compute_rot);
+cudaError_t launch_prep(const Params& prm, const Ptrs& P, int compute_rot, int max_nm, cudaStream_t st) {
+  dim3 grid(grid_for(max_nm, 256), prm.nmem);
+  k_prep<<<grid, 256, 0, st>>>(prm, P, compute_rot);
   return cudaGetLastError();
 }
 cudaError_t launch_dts(const Params& prm, const Ptrs& P, int compute_rot, int first, cudaStream_t st) {
-  k_dts<<<1, 1, 0, st>>>(prm, P, compute_rot, first);
+  k_dts<<<1, 256, 0, st>>>(prm, P, compute_rot, first);
   return cudaGetLastError();
 }
 cudaError_t launch_sice(const Params& prm, const Ptrs& P, cudaStream_t st) {
-  k_sice<<<(prm.N + 127) / 128, 128, 0, st>>>(prm, P);
+  k_sice<<<(prm.Ntot + 127) / 128, 128, 0, st>>>(prm, P);
   return cudaGetLastError();
 }
 cudaError_t launch_diag(const Params& prm, const Ptrs& P, cudaStream_t st) {
-  k_diag<<<(prm.N + 127) / 128, 128, 0, st>>>(prm, P);
+  k_diag<<<(prm.Ntot + 127) / 128, 128, 0, st>>>(prm, P);
   return cudaGetLastError();
 }
 cudaError_t launch_stokes(const Params& prm, const Ptrs& P, cudaStream_t st) {
-  k_stokes<<<(prm.N + 127) / 128, 128, 0, st>>>(prm, P);
+  k_stokes<<<(prm.Ntot + 127) / 128, 128, 0, st>>>(prm, P);
   return cudaGetLastError();
 }
 cudaError_t launch_screen(const Params& prm, const Ptrs& P, cudaStream_t st) {
-  k_screen<<<1, 256, 0, st>>>(prm, P);
+  k_screen<<<prm.nmem, 256, 0, st>>>(prm, P);
   return cudaGetLastError();
 }
-cudaError_t launch_to_ref(const Params& prm, const float* E, float* F, cudaStream_t st) {
-  dim3 grid((prm.O * prm.P + 31) / 32, (prm.N + 31) / 32), block(32, 8);
-  k_to_ref<<<grid, block, 0, st>>>(prm, E, F);
+cudaError_t launch_to_ref(const Params& prm, const float* E, float* F, int off, int n, cudaStream_t st) {
+  dim3 grid((prm.O * prm.P + 31) / 32, (n + 31) / 32), block(32, 8);
+  k_to_ref<<<grid, block, 0, st>>>(prm, E, F, off, n);
   return cudaGetLastError();
 }
-cudaError_t launch_from_ref(const Params& prm, const float* F, float* E, cudaStream_t st) {
-  dim3 grid((prm.O * prm.P + 31) / 32, (prm.N + 31) / 32), block(32, 8);
-  k_from_ref<<<grid, block, 0, st>>>(prm, F, E);
+cudaError_t launch_from_ref(const Params& prm, const float* F, float* E, int off, int n, cudaStream_t st) {
+  dim3 grid((prm.O * prm.P + 31) / 32, (n + 31) / 32), block(32, 8);
+  k_from_ref<<<grid, block, 0, st>>>(prm, F, E, off, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_begin_dtg(const Params& prm, cudaStream_t st) {
+  k_begin_dtg<<<1, 256, 0, st>>>(prm);
   return cudaGetLastError();
 }
 cudaError_t launch_fill(float* a, size_t n, float v, cudaStream_t st) {

@@ -31,7 +31,7 @@
 
 namespace umwm {
 
-constexpr int PTS = 64;  // wet points per CTA (4 warps x 16)
+constexpr int PTS = TILE;  // wet points per CTA (4 warps x 16)
 
 // bulk prefetch of a contiguous, 16-byte aligned range into L2 (sizes are multiples of 16 bytes)
 __device__ __forceinline__ void bulk_prefetch_l2(const void* p, unsigned bytes) {
@@ -98,18 +98,24 @@ template <int H, bool INTEG>
 __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm, const Ptrs P, int compute_rot) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int j16 = lane & 15, half = lane >> 4;
-  const int N = prm.N, O = prm.O;
+  const int O = prm.O;
+  const Member& Mb = prm.mem[prm.tile_mem[blockIdx.x]];
+  Ctl* ctl = Mb.ctl;
+  // members that have finished the current dtg sit the substep out
+  if (INTEG ? !ctl->running : ctl->done) return;
+  const int N = Mb.ghost;  // this member's ghost point (its wet points end here)
   const int j = blockIdx.x * PTS + w * 16 + j16;
   const bool valid = j < N;
-  const int jj = valid ? j : N;  // the ghost column keeps loads in bounds
+  const int jj = valid ? j : N;  // the ghost keeps loads in bounds
+  const int ja = apt(Mb, jj);
   const float sg = half ? -1.f : 1.f;
   __shared__ float cws[H][128];
 
-  const float dts = INTEG ? P.ctl->dts : 0.f;
+  const float dts = INTEG ? ctl->dts : 0.f;
   const float ustar = P.ustar[jj];
-  const WindIn wi = load_wind(prm, P, jj, ustar);
-  const float wdir = P.wdir[jj];
-  const float sdtc = (prm.sdt_fac * sqrtf(P.rhorat[jj])) * ustar;
+  const WindIn wi = load_wind(prm, P, jj, ja, ustar);
+  const float wdir = P.wdir[ja];
+  const float sdtc = (prm.sdt_fac * sqrtf(P.rhorat[ja])) * ustar;
   const float sv = prm.ice_possible ? P.sice_v[jj] : 0.f;
   const float hdth = 0.5f * prm.dth;
   const float ucg = sg * wi.uc, vcg = sg * wi.vc;
@@ -120,7 +126,7 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
   int nie = N, niw = N, nin = N, nis = N;
   float vce = 0.f, vcw = 0.f, ucn = 0.f, ucs = 0.f, odx = 0.f, ody = 0.f;
   if (!INTEG && compute_rot) {
-    nie = P.ie[jj]; niw = P.iw[jj]; nin = P.in[jj]; nis = P.is[jj];
+    nie = P.ie[jj]; niw = P.iw[jj]; nin = P.in[jj]; nis = P.is[jj];  // global indices
     vce = P.vc[P.iie[jj]]; vcw = P.vc[P.iiw[jj]]; ucn = P.uc[P.iin[jj]]; ucs = P.uc[P.iis[jj]];
     odx = P.oneovdx[jj]; ody = P.oneovdy[jj];
   }
@@ -151,7 +157,7 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
     if (o < O) {
       const float* r = Eb + (size_t)o * lstride;
 #pragma unroll
-      for (int k = 0; k < H; ++k) ec[k] = __ldg(r + k * 32);
+      for (int k = 0; k < H; ++k) ec[k] = r[k * 32];  // E is also written (as ef) by this kernel
       const bool prog = o < wi.oc;
       const Level<H> Lc = load_level<H>(prm, Tb + (size_t)o * tstride, !INTEG && prog);
       Cc.a = A; Cc.b = B; Cc.c = C;
@@ -263,19 +269,19 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
     float bm = valid ? ph : __int_as_float(0x7f800000);
 #pragma unroll
     for (int s = 8; s > 0; s >>= 1) bm = fminf(bm, __shfl_xor_sync(0xffffffffu, bm, s));
-    if (lane == 0) atomicMin(&P.ctl->minphys_enc, enc_ord_d(bm));
+    if (lane == 0) atomicMin(&ctl->minphys_enc, enc_ord_d(bm));
     if (compute_rot) {
       float m = valid ? rmx : 0.f;
 #pragma unroll
       for (int s = 16; s > 0; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
-      if (lane == 0) atomicMax(&P.ctl->maxrot_enc, enc_ord_d(m));
+      if (lane == 0) atomicMax(&ctl->maxrot_enc, enc_ord_d(m));
     }
   }
 }
 
 template <bool INTEG>
 static cudaError_t launch_source_t(const Params& prm, const Ptrs& P, int compute_rot, cudaStream_t st) {
-  dim3 grid((prm.N + PTS - 1) / PTS), block(128);
+  dim3 grid(prm.ntiles), block(128);
   switch (prm.P / 2) {
 #define CASE(X) \
   case X: k_source<X, INTEG><<<grid, block, 0, st>>>(prm, P, compute_rot); break;

@@ -7,7 +7,7 @@
 namespace umwm {
 
 bool supported_pm(int pm);
-cudaError_t launch_prep(const Params& prm, const Ptrs& P, int compute_rot, cudaStream_t st);
+cudaError_t launch_prep(const Params& prm, const Ptrs& P, int compute_rot, int max_nm, cudaStream_t st);
 cudaError_t launch_sice(const Params& prm, const Ptrs& P, cudaStream_t st);
 cudaError_t launch_source_phys(const Params& prm, const Ptrs& P, int compute_rot, cudaStream_t st);
 cudaError_t launch_dts(const Params& prm, const Ptrs& P, int compute_rot, int first, cudaStream_t st);
@@ -16,8 +16,9 @@ cudaError_t launch_advect(const Params& prm, const Ptrs& P, cudaStream_t st);
 cudaError_t launch_diag(const Params& prm, const Ptrs& P, cudaStream_t st);
 cudaError_t launch_stokes(const Params& prm, const Ptrs& P, cudaStream_t st);
 cudaError_t launch_screen(const Params& prm, const Ptrs& P, cudaStream_t st);
-cudaError_t launch_to_ref(const Params& prm, const float* E, float* F, cudaStream_t st);
-cudaError_t launch_from_ref(const Params& prm, const float* F, float* E, cudaStream_t st);
+cudaError_t launch_to_ref(const Params& prm, const float* E, float* F, int off, int n, cudaStream_t st);
+cudaError_t launch_from_ref(const Params& prm, const float* F, float* E, int off, int n, cudaStream_t st);
+cudaError_t launch_begin_dtg(const Params& prm, cudaStream_t st);
 cudaError_t launch_fill(float* a, size_t n, float v, cudaStream_t st);
 
 }  // namespace umwm

@@ -68,44 +68,66 @@ struct Dev {
   }
 };
 
-struct Model {
+// One member of the model (a single domain is a one-member ensemble).
+struct MemberHost {
   HostModel H;
+  Inputs in;              // this member's stand-ins for the reference's files
+  bool readfile = false;  // any forcing variable comes from the input files
+  int off = 0, N = 0, ghost = 0, padded = 0, nmoff = 0, NM = 0;
+  Ctl* ctl = nullptr;
+  double* log = nullptr;
+  int log_cap = 0;
+  int *mi = nullptr, *ni = nullptr;
+  float *uwb = nullptr, *uwf = nullptr, *vwb = nullptr, *vwf = nullptr, *ucb = nullptr, *ucf = nullptr,
+        *vcb = nullptr, *vcf = nullptr, *rhoab = nullptr, *rhoaf = nullptr, *rhowb = nullptr, *rhowf = nullptr,
+        *ficeb = nullptr, *ficef = nullptr;
+  size_t screen_printed = 0;
+  int substep_mark = 0;  // member substep counter at the start of the last run
+};
+
+struct Model {
+  std::vector<MemberHost> mem;
   bool on_device = false;
   Params prm{};
   Ptrs P{};
   std::unique_ptr<Dev> dev;
+  Member* d_mem = nullptr;
+  int* d_tile_mem = nullptr;
+  Global* d_glob = nullptr;
   cudaStream_t st = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  int* done_h = nullptr;  // pinned
-  bool first = true, firstdtg = true, readfile = false;
+  int* flag_h = nullptr;  // pinned read-back of Global::not_done
+  bool first = true;
   long long substeps = 0, max_substeps = -1;
   bool verbose = false, check_finite = false, use_graph = false;
   double last_gpu_ms = 0, last_bins = 0;
   long long launches = 0;
-  size_t screen_printed = 0;
+  int sel = 0;      // member the getters and setters act on
+  int max_nm = 0;   // largest all-point range of a member
   bool ktime = false;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> kev;  // pending (kernel, events)
   std::vector<cudaEvent_t> evpool;
   size_t evused = 0;
   double kms[K_NK] = {0};
   long long kcnt[K_NK] = {0};
-  // forcing levels on the device (mm*nm each)
-  float *uwb = nullptr, *uwf = nullptr, *vwb = nullptr, *vwf = nullptr, *ucb = nullptr, *ucf = nullptr,
-        *vcb = nullptr, *vcf = nullptr, *rhoab = nullptr, *rhoaf = nullptr, *rhowb = nullptr, *rhowf = nullptr,
-        *ficeb = nullptr, *ficef = nullptr;
-  // writable views of the Ptrs members
-  float *E = nullptr, *ES = nullptr, *EF = nullptr, *TAB = nullptr;
+  float *E = nullptr, *ES = nullptr, *TAB = nullptr;
 
   ~Model() {
     for (cudaEvent_t e : evpool) cudaEventDestroy(e);
     if (st) cudaStreamDestroy(st);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
-    if (done_h) cudaFreeHost(done_h);
+    if (flag_h) cudaFreeHost(flag_h);
   }
 };
 
 std::unique_ptr<Model> g_model;
+
+struct Pending {  // a member added with umwm_gpu_ensemble_add, not yet initialized
+  std::string nml;
+  Inputs in;
+};
+std::vector<Pending> g_pending;
 
 cudaEvent_t next_event(Model& M) {
   if (M.evused == M.evpool.size()) {
@@ -141,118 +163,168 @@ void collect_timings(Model& M) {
   M.evused = 0;
 }
 
-// per-(o,i) tables in the blocked device layout [o][j/32][t][32]; ghost
-// point N holds the ghost values of cp0/cg0; points past N get finite
-// throw-away values (k = 1) so that idle lanes stay finite
-std::vector<float> build_tables(const HostModel& H, const Params& prm) {
-  const int O = H.om, N = H.im;
+// per-(o,i) tables in the blocked device layout [o][j/32][t][32].  A member's
+// ghost point holds the ghost values of cp0/cg0; padding points get finite
+// throw-away values (k = 1) so that idle lanes stay finite.
+std::vector<float> build_tables(const Model& M) {
+  const Params& prm = M.prm;
+  const int O = prm.O;
   std::vector<float> T((size_t)O * prm.NB * T_COUNT * 32, 0.f);
-  const std::vector<float>* src[T_COUNT] = {&H.k, &H.cp0, &H.cg0, &H.logl2overz, &H.fkovg, &H.k4, &H.k3dk,
-                                            &H.kdk, &H.cothkd, &H.sbf, &H.sdv, &H.bf1r, &H.bf2r};
-  for (int o = 1; o <= O; ++o)
-    for (int t = 0; t < T_COUNT; ++t) {
-      const bool ghost = (t == T_CP0 || t == T_CG0);
-      for (int j = 0; j < prm.ldN; ++j) {
-        float v;
-        if (j < N) v = (*src[t])[H.oi(o, j + 1)];
-        else if (ghost) v = (*src[t])[H.oi(o, 0)];
-        else v = (t == T_K || t == T_K4 || t == T_KDK || t == T_COTHKD) ? 1.f : 0.f;
-        T[tidx(prm, o - 1, t, j)] = v;
+  for (const MemberHost& mh : M.mem) {
+    const HostModel& H = mh.H;
+    const std::vector<float>* src[T_COUNT] = {&H.k, &H.cp0, &H.cg0, &H.logl2overz, &H.fkovg, &H.k4, &H.k3dk,
+                                              &H.kdk, &H.cothkd, &H.sbf, &H.sdv, &H.bf1r, &H.bf2r};
+    for (int o = 1; o <= O; ++o)
+      for (int t = 0; t < T_COUNT; ++t) {
+        const bool ghost = (t == T_CP0 || t == T_CG0);
+        for (int j = 0; j < mh.padded; ++j) {
+          float v;
+          if (j < mh.N) v = (*src[t])[H.oi(o, j + 1)];
+          else if (ghost) v = (*src[t])[H.oi(o, 0)];
+          else v = (t == T_K || t == T_K4 || t == T_KDK || t == T_COTHKD) ? 1.f : 0.f;
+          T[tidx(prm, o - 1, t, mh.off + j)] = v;
+        }
       }
-    }
+  }
   return T;
 }
 
-int set_forcing_constants(Model& M) {
+int set_forcing_constants(Model& M, MemberHost& mh) {
   // input_nc without file variables: umwm_io.F90:39-83
-  const HostModel& H = M.H;
-  const size_t NM = H.imm;
+  const HostModel& H = mh.H;
+  const size_t NM = mh.NM, a = mh.nmoff;
   if (!H.winds) {
-    CU(launch_fill(M.P.wspd, NM, H.wspd0, M.st));
-    CU(launch_fill(M.P.wdir, NM, H.wdir0, M.st));
+    CU(launch_fill(M.P.wspd + a, NM, H.wspd0, M.st));
+    CU(launch_fill(M.P.wdir + a, NM, H.wdir0, M.st));
   }
   if (!H.currents) {
-    CU(launch_fill(M.P.uc, NM, H.uc0, M.st));
-    CU(launch_fill(M.P.vc, NM, H.vc0, M.st));
+    CU(launch_fill(M.P.uc + a, NM, H.uc0, M.st));
+    CU(launch_fill(M.P.vc + a, NM, H.vc0, M.st));
   }
-  if (!H.seaice) CU(launch_fill(M.P.fice, NM, H.fice0, M.st));
-  if (!H.air_density) CU(launch_fill(M.P.rhoa, NM, H.rhoa0, M.st));
-  if (!H.water_density) CU(launch_fill(M.P.rhow, NM, H.rhow0, M.st));
+  if (!H.seaice) CU(launch_fill(M.P.fice + a, NM, H.fice0, M.st));
+  if (!H.air_density) CU(launch_fill(M.P.rhoa + a, NM, H.rhoa0, M.st));
+  if (!H.water_density) CU(launch_fill(M.P.rhow + a, NM, H.rhow0, M.st));
   return UMWM_OK;
 }
 
 // input_nc(timestr) file variables into the n+1 level, umwm_io.F90:13-93
-int read_forcing(Model& M, const std::string& key, std::vector<float>* uwf_host = nullptr,
+int read_forcing(Model& M, MemberHost& mh, const std::string& key, std::vector<float>* uwf_host = nullptr,
                  std::vector<float>* vwf_host = nullptr) {
-  const HostModel& H = M.H;
-  if (!M.readfile) return UMWM_OK;
-  auto it = g_inputs.forcing.find(key);
-  if (it == g_inputs.forcing.end()) return fail(UMWM_ERR_INPUT, "input_nc: no forcing staged for " + key);
+  const HostModel& H = mh.H;
+  if (!mh.readfile) return UMWM_OK;
+  auto it = mh.in.forcing.find(key);
+  if (it == mh.in.forcing.end()) return fail(UMWM_ERR_INPUT, "input_nc: no forcing staged for " + key);
   const size_t n2 = (size_t)H.mm * H.nm;
   auto get = [&](const char* var, float* dst, bool zero_land, std::vector<float>* keep) -> int {
     auto v = it->second.find(var);
     if (v == it->second.end()) return fail(UMWM_ERR_INPUT, std::string("input_nc: variable ") + var + " missing for " + key);
     if (v->second.size() != n2) return fail(UMWM_ERR_INPUT, std::string("input_nc: variable ") + var + " has the wrong size");
-    std::vector<float> tmp = v->second;
-    if (zero_land)
+    const float* src = v->second.data();
+    std::vector<float> tmp;
+    if (zero_land) {
+      tmp = v->second;
       for (size_t q = 0; q < n2; ++q) if (H.mask[q] == 0) tmp[q] = 0.f;
-    if (keep) *keep = tmp;
-    CU(cudaMemcpyAsync(dst, tmp.data(), n2 * 4, cudaMemcpyHostToDevice, M.st));
+      src = tmp.data();
+    }
+    if (keep) keep->assign(src, src + n2);
+    CU(cudaMemcpyAsync(dst, src, n2 * 4, cudaMemcpyHostToDevice, M.st));
     CU(cudaStreamSynchronize(M.st));
     return UMWM_OK;
   };
   int rc;
   if (H.winds) {
-    if ((rc = get("uw", M.uwf, false, uwf_host))) return rc;
-    if ((rc = get("vw", M.vwf, false, vwf_host))) return rc;
+    if ((rc = get("uw", mh.uwf, false, uwf_host))) return rc;
+    if ((rc = get("vw", mh.vwf, false, vwf_host))) return rc;
   }
   if (H.currents) {
-    if ((rc = get("uc", M.ucf, true, nullptr))) return rc;
-    if ((rc = get("vc", M.vcf, true, nullptr))) return rc;
+    if ((rc = get("uc", mh.ucf, true, nullptr))) return rc;
+    if ((rc = get("vc", mh.vcf, true, nullptr))) return rc;
   }
-  if (H.seaice && (rc = get("fice", M.ficef, false, nullptr))) return rc;
-  if (H.air_density && (rc = get("rhoa", M.rhoaf, false, nullptr))) return rc;
-  if (H.water_density && (rc = get("rhow", M.rhowf, false, nullptr))) return rc;
+  if (H.seaice && (rc = get("fice", mh.ficef, false, nullptr))) return rc;
+  if (H.air_density && (rc = get("rhoa", mh.rhoaf, false, nullptr))) return rc;
+  if (H.water_density && (rc = get("rhow", mh.rhowf, false, nullptr))) return rc;
   return UMWM_OK;
 }
 
 // forcinginput, umwm_forcing.F90:11-37
-int forcing_input(Model& M, const std::string& key) {
-  const HostModel& H = M.H;
+int forcing_input(Model& M, MemberHost& mh, const std::string& key) {
+  const HostModel& H = mh.H;
   const size_t b = (size_t)H.mm * H.nm * 4;
-  if (H.winds) { CU(cudaMemcpyAsync(M.uwb, M.uwf, b, cudaMemcpyDeviceToDevice, M.st)); CU(cudaMemcpyAsync(M.vwb, M.vwf, b, cudaMemcpyDeviceToDevice, M.st)); }
-  if (H.currents) { CU(cudaMemcpyAsync(M.ucb, M.ucf, b, cudaMemcpyDeviceToDevice, M.st)); CU(cudaMemcpyAsync(M.vcb, M.vcf, b, cudaMemcpyDeviceToDevice, M.st)); }
-  if (H.air_density) CU(cudaMemcpyAsync(M.rhoab, M.rhoaf, b, cudaMemcpyDeviceToDevice, M.st));
-  if (H.water_density) CU(cudaMemcpyAsync(M.rhowb, M.rhowf, b, cudaMemcpyDeviceToDevice, M.st));
-  if (H.seaice) CU(cudaMemcpyAsync(M.ficeb, M.ficef, b, cudaMemcpyDeviceToDevice, M.st));
-  int rc = read_forcing(M, key);
+  auto cp = [&](float* d, const float* s_) { return cudaMemcpyAsync(d, s_, b, cudaMemcpyDeviceToDevice, M.st); };
+  if (H.winds) { CU(cp(mh.uwb, mh.uwf)); CU(cp(mh.vwb, mh.vwf)); }
+  if (H.currents) { CU(cp(mh.ucb, mh.ucf)); CU(cp(mh.vcb, mh.vcf)); }
+  if (H.air_density) CU(cp(mh.rhoab, mh.rhoaf));
+  if (H.water_density) CU(cp(mh.rhowb, mh.rhowf));
+  if (H.seaice) CU(cp(mh.ficeb, mh.ficef));
+  int rc = read_forcing(M, mh, key);
   if (rc) return rc;
-  if (M.readfile) return set_forcing_constants(M);
+  if (mh.readfile) return set_forcing_constants(M, mh);
   return UMWM_OK;
 }
 
+// Parameters shared by all members; members must agree on them.
 int setup_params(Model& M) {
-  HostModel& H = M.H;
+  const HostModel& H = M.mem[0].H;
+  for (size_t m = 1; m < M.mem.size(); ++m) {
+    const HostModel& G = M.mem[m].H;
+    const bool same =
+        G.om == H.om && G.pm == H.pm && G.fmin == H.fmin && G.fmax == H.fmax && G.fprog == H.fprog && G.dtg == H.dtg &&
+        G.g == H.g && G.nu_air == H.nu_air && G.nu_water == H.nu_water && G.sfct == H.sfct && G.kappa == H.kappa &&
+        G.z == H.z && G.explim == H.explim && G.sin_fac == H.sin_fac && G.sin_diss1 == H.sin_diss1 &&
+        G.sin_diss2 == H.sin_diss2 && G.sds_fac == H.sds_fac && G.sds_power == H.sds_power && G.mss_fac == H.mss_fac &&
+        G.snl_fac == H.snl_fac && G.sdt_fac == H.sdt_fac && G.sbf_fac == H.sbf_fac && G.sbp_fac == H.sbp_fac &&
+        G.winds == H.winds && G.currents == H.currents && G.air_density == H.air_density &&
+        G.water_density == H.water_density && G.seaice == H.seaice && G.restart == H.restart && G.stokes == H.stokes &&
+        G.fice_lth == H.fice_lth && G.fice_uth == H.fice_uth && G.rhow0 == H.rhow0 && G.depth == H.depth &&
+        G.starttimestr == H.starttimestr;
+    if (!same)
+      return fail(UMWM_ERR_UNSUPPORTED, "ensemble members must share the spectral grid, physics, forcing switches, "
+                                        "dtg, start time and Stokes depths; member " + std::to_string(m) + " differs");
+  }
   if (H.om > MAX_OM) return fail(UMWM_ERR_UNSUPPORTED, "om > 64 is not supported");
   if (H.pm > MAX_PM || !supported_pm(H.pm))
-    return fail(UMWM_ERR_UNSUPPORTED, "pm must be 4*k with k in {2,3,4,6,8,9,12,16,18}");
+    return fail(UMWM_ERR_UNSUPPORTED, "pm must be 4*k with k in {2,3,4,6,8,9,12}");
   if (H.lm > MAX_LM) return fail(UMWM_ERR_UNSUPPORTED, "more than 100 Stokes depths");
-  if (H.gustiness > 0) return fail(UMWM_ERR_UNSUPPORTED, "gustiness > 0 (Fortran random_number) is not supported");
+  for (const MemberHost& mh : M.mem)
+    if (mh.H.gustiness > 0)
+      return fail(UMWM_ERR_UNSUPPORTED, "gustiness > 0 (Fortran random_number) is not supported");
   Params& p = M.prm;
-  p.N = H.im;
-  p.NB = (H.im + 1 + 31) / 32;
-  p.ldN = p.NB * 32;
-  p.O = H.om; p.P = H.pm; p.NM = H.imm; p.mm = H.mm; p.nm = H.nm; p.lm = H.lm;
-  p.iip = (H.iip >= 1 && H.iip <= H.im) ? H.iip - 1 : -1;
+  // layout: each member's wet points, its ghost, padding to a tile
+  int off = 0, nmoff = 0;
+  M.max_nm = 0;
+  for (MemberHost& mh : M.mem) {
+    mh.N = mh.H.im;
+    mh.off = off;
+    mh.ghost = off + mh.N;
+    mh.padded = (mh.N + 1 + TILE - 1) / TILE * TILE;
+    off += mh.padded;
+    mh.NM = mh.H.imm;
+    mh.nmoff = nmoff;
+    nmoff += mh.NM;
+    M.max_nm = std::max(M.max_nm, mh.NM);
+    mh.readfile = mh.H.winds || mh.H.currents || mh.H.air_density || mh.H.water_density || mh.H.seaice;
+  }
+  p.Ntot = off;
+  p.NB = off / 32;
+  p.ldN = off;
+  p.NMtot = nmoff;
+  p.ntiles = off / TILE;
+  p.nmem = (int)M.mem.size();
+  p.O = H.om; p.P = H.pm; p.lm = H.lm;
   p.g = H.g; p.explim = H.explim; p.sin_fac = H.sin_fac; p.fieldscale1 = H.fieldscale1;
   p.fieldscale2 = H.fieldscale2; p.twopisds_fac = H.twopisds_fac; p.sds_power = H.sds_power;
   p.inv_sds_power = H.inv_sds_power; p.mss_fac = H.mss_fac; p.snl_fac = H.snl_fac; p.sdt_fac = H.sdt_fac;
   p.z = H.z; p.nu_air = H.nu_air; p.kappa = H.kappa; p.fprog = H.fprog; p.dth = H.dth; p.dthg = H.dthg;
-  p.oneovdth = H.oneovdth; p.dtamin = H.dtamin; p.dtg = H.dtg; p.fice_lth = H.fice_lth; p.fice_uth = H.fice_uth;
+  p.oneovdth = H.oneovdth; p.dtg = H.dtg; p.fice_lth = H.fice_lth; p.fice_uth = H.fice_uth;
   p.eulerinv = H.eulerinv; p.rhow0 = H.rhow0;
   p.winds = H.winds; p.currents = H.currents; p.air_density = H.air_density; p.water_density = H.water_density;
-  p.seaice = H.seaice; p.restart = H.restart; p.curvilinear = H.curvilinear; p.isglobal = H.isglobal;
-  p.ice_possible = H.seaice || (H.fice0 > H.fice_lth);
+  p.seaice = H.seaice; p.restart = H.restart;
+  p.curvilinear = 0; p.isglobal = 0; p.ice_possible = 0;
+  for (const MemberHost& mh : M.mem) {
+    p.curvilinear |= mh.H.curvilinear;
+    p.isglobal |= mh.H.isglobal;
+    p.ice_possible |= (mh.H.seaice || (mh.H.fice0 > mh.H.fice_lth));
+  }
   for (int o = 0; o < H.om; ++o) { p.f[o] = H.f[o]; p.dom[o] = H.dom[o]; }
   for (int q = 0; q < H.pm; ++q) {
     p.th[q] = H.th[q]; p.cth[q] = H.cth[q]; p.sth[q] = H.sth[q];
@@ -264,11 +336,10 @@ int setup_params(Model& M) {
 }
 
 int init_device(Model& M) {
-  HostModel& H = M.H;
   int rc = setup_params(M);
   if (rc) return rc;
-  const Params& p = M.prm;
-  const int N = p.N, ldN = p.ldN, NM = p.NM;
+  Params& p = M.prm;
+  const int ldN = p.ldN;
   const size_t spec = (size_t)p.O * p.P * ldN;
   if (g_device >= 0) CU(cudaSetDevice(g_device));
   M.dev.reset(new Dev());
@@ -276,164 +347,218 @@ int init_device(Model& M) {
   CU(cudaStreamCreateWithFlags(&M.st, cudaStreamNonBlocking));
   CU(cudaEventCreate(&M.ev0));
   CU(cudaEventCreate(&M.ev1));
-  CU(cudaMallocHost(&M.done_h, sizeof(int)));
+  CU(cudaMallocHost(&M.flag_h, sizeof(int)));
   Ptrs& P = M.P;
   CU(D.alloc(&M.E, spec, false));
   CU(D.alloc(&M.ES, spec, false));
-  CU(D.alloc(&M.EF, spec, false));
-  P.E = M.E; P.ES = M.ES; P.EF = M.EF;
+  P.E = M.E; P.ES = M.ES;
+  P.EF = M.E;  // ef overwrites e bin by bin (source integration), e overwrites ef (advection)
   CU(D.alloc(&M.TAB, (size_t)p.O * T_COUNT * ldN, false));
   P.TAB = M.TAB;
   {
-    std::vector<float> T = build_tables(H, p);
+    std::vector<float> T = build_tables(M);
     CU(cudaMemcpy(M.TAB, T.data(), T.size() * 4, cudaMemcpyHostToDevice));
   }
-  // wet-point integer arrays
-  auto upload_i = [&](const int** dst, const std::vector<int>& src, bool aliased) -> int {
-    std::vector<int> h(ldN, aliased ? N : 0);
-    for (int i = 1; i <= N; ++i) {
-      int v = src[i];
-      h[i - 1] = aliased ? (v == 0 ? N : v - 1) : v - 1;
+  // per-point arrays in the common index space
+  auto upload_i = [&](const int** dst, std::vector<int>(HostModel::*field), bool aliased) -> int {
+    std::vector<int> h(ldN, 0);
+    for (const MemberHost& mh : M.mem) {
+      const std::vector<int>& src = mh.H.*field;
+      for (int j = 0; j < mh.padded; ++j) {
+        int v;
+        if (j < mh.N) {
+          const int r = src[j + 1];
+          v = aliased ? (r == 0 ? mh.ghost : mh.off + r - 1) : mh.nmoff + r - 1;
+        } else {
+          v = aliased ? mh.ghost : mh.nmoff + mh.N;  // the member's ghost / a land point
+        }
+        h[mh.off + j] = v;
+      }
     }
     int* d = nullptr;
     CU(D.alloc(&d, ldN));
-    CU(cudaMemcpy(d, h.data(), ldN * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(d, h.data(), (size_t)ldN * 4, cudaMemcpyHostToDevice));
     *dst = d;
     return UMWM_OK;
   };
-  if ((rc = upload_i(&P.ie, H.ie, true)) || (rc = upload_i(&P.iw, H.iw, true)) ||
-      (rc = upload_i(&P.in, H.in, true)) || (rc = upload_i(&P.is, H.is, true)) ||
-      (rc = upload_i(&P.iie, H.iie, false)) || (rc = upload_i(&P.iiw, H.iiw, false)) ||
-      (rc = upload_i(&P.iin, H.iin, false)) || (rc = upload_i(&P.iis, H.iis, false)))
+  if ((rc = upload_i(&P.ie, &HostModel::ie, true)) || (rc = upload_i(&P.iw, &HostModel::iw, true)) ||
+      (rc = upload_i(&P.in, &HostModel::in, true)) || (rc = upload_i(&P.is, &HostModel::is, true)) ||
+      (rc = upload_i(&P.iie, &HostModel::iie, false)) || (rc = upload_i(&P.iiw, &HostModel::iiw, false)) ||
+      (rc = upload_i(&P.iin, &HostModel::iin, false)) || (rc = upload_i(&P.iis, &HostModel::iis, false)))
     return rc;
-  auto upload_f = [&](const float** dst, const std::vector<float>& src) -> int {
+  auto upload_f = [&](const float** dst, std::vector<float>(HostModel::*field)) -> int {
     std::vector<float> h(ldN, 1.f);
-    for (int i = 1; i <= N; ++i) h[i - 1] = src[i];
+    for (const MemberHost& mh : M.mem) {
+      const std::vector<float>& src = mh.H.*field;
+      for (int i = 1; i <= mh.N; ++i) h[mh.off + i - 1] = src[i];
+    }
     float* d = nullptr;
     CU(D.alloc(&d, ldN));
-    CU(cudaMemcpy(d, h.data(), ldN * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(d, h.data(), (size_t)ldN * 4, cudaMemcpyHostToDevice));
     *dst = d;
     return UMWM_OK;
   };
-  if ((rc = upload_f(&P.oneovar, H.oneovar)) || (rc = upload_f(&P.oneovdx, H.oneovdx)) ||
-      (rc = upload_f(&P.oneovdy, H.oneovdy)) || (rc = upload_f(&P.dxn, H.dxn)) || (rc = upload_f(&P.dxs, H.dxs)) ||
-      (rc = upload_f(&P.dye, H.dye)) || (rc = upload_f(&P.dyw, H.dyw)) || (rc = upload_f(&P.d, H.d)) ||
-      (rc = upload_f(&P.curv, H.curv_i)))
+  if ((rc = upload_f(&P.oneovar, &HostModel::oneovar)) || (rc = upload_f(&P.oneovdx, &HostModel::oneovdx)) ||
+      (rc = upload_f(&P.oneovdy, &HostModel::oneovdy)) || (rc = upload_f(&P.dxn, &HostModel::dxn)) ||
+      (rc = upload_f(&P.dxs, &HostModel::dxs)) || (rc = upload_f(&P.dye, &HostModel::dye)) ||
+      (rc = upload_f(&P.dyw, &HostModel::dyw)) || (rc = upload_f(&P.d, &HostModel::d)) ||
+      (rc = upload_f(&P.curv, &HostModel::curv_i)))
     return rc;
   {
     std::vector<int> ones(ldN, 1);
     CU(D.alloc(&P.oc, ldN)); CU(D.alloc(&P.oc_rot, ldN));
-    CU(cudaMemcpy(P.oc, ones.data(), ldN * 4, cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(P.oc_rot, ones.data(), ldN * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(P.oc, ones.data(), (size_t)ldN * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(P.oc_rot, ones.data(), (size_t)ldN * 4, cudaMemcpyHostToDevice));
   }
   for (float** q : {&P.ustar, &P.cd, &P.taux, &P.tauy, &P.taux_form, &P.tauy_form, &P.taux_skin, &P.tauy_skin,
                     &P.taux_diag, &P.tauy_diag, &P.tailatmx, &P.tailatmy, &P.shelt, &P.fcutoff, &P.phys, &P.sice_v,
                     &P.ds, &P.ht, &P.mwp, &P.mwd, &P.mss, &P.mwl, &P.dwd, &P.dwl, &P.dwp, &P.dcp0, &P.dcp, &P.dcg0,
                     &P.dcg, &P.momx, &P.momy, &P.cgmxx, &P.cgmxy, &P.cgmyy})
     CU(D.alloc(q, ldN));
-  for (float** q : {&P.wspd, &P.wdir, &P.uc, &P.vc, &P.rhoa, &P.rhow, &P.rhorat, &P.fice}) CU(D.alloc(q, NM));
-  {
-    std::vector<int> mi(NM), ni(NM);
-    for (int i = 1; i <= NM; ++i) { mi[i - 1] = H.mi[i]; ni[i - 1] = H.ni[i]; }
-    int *dmi, *dni;
-    CU(D.alloc(&dmi, NM)); CU(D.alloc(&dni, NM));
-    CU(cudaMemcpy(dmi, mi.data(), NM * 4, cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(dni, ni.data(), NM * 4, cudaMemcpyHostToDevice));
-    P.mi = dmi; P.ni = dni;
+  for (float** q : {&P.wspd, &P.wdir, &P.uc, &P.vc, &P.rhoa, &P.rhow, &P.rhorat, &P.fice}) CU(D.alloc(q, p.NMtot));
+  CU(D.alloc(&P.us, (size_t)std::max(1, p.lm) * ldN));
+  CU(D.alloc(&P.vs, (size_t)std::max(1, p.lm) * ldN));
+  CU(D.alloc(&M.d_glob, 1));
+  P.glob = M.d_glob;
+  // per-member device pieces
+  Ctl* ctls = nullptr;
+  CU(D.alloc(&ctls, M.mem.size()));
+  std::vector<Member> hm(M.mem.size());
+  for (size_t m = 0; m < M.mem.size(); ++m) {
+    MemberHost& mh = M.mem[m];
+    const HostModel& H = mh.H;
+    mh.ctl = ctls + m;
+    mh.log_cap = M.mem.size() > 1 ? (1 << 14) : (1 << 20);
+    CU(D.alloc(&mh.log, (size_t)mh.log_cap * 8));
+    std::vector<int> mi(mh.NM), ni(mh.NM);
+    for (int i = 1; i <= mh.NM; ++i) { mi[i - 1] = H.mi[i]; ni[i - 1] = H.ni[i]; }
+    CU(D.alloc(&mh.mi, mh.NM)); CU(D.alloc(&mh.ni, mh.NM));
+    CU(cudaMemcpy(mh.mi, mi.data(), (size_t)mh.NM * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(mh.ni, ni.data(), (size_t)mh.NM * 4, cudaMemcpyHostToDevice));
+    const size_t n2 = (size_t)H.mm * H.nm;
+    auto lev = [&](bool on, float** b, float** f) -> int {
+      if (!on) return UMWM_OK;
+      CU(D.alloc(b, n2)); CU(D.alloc(f, n2));
+      return UMWM_OK;
+    };
+    if ((rc = lev(H.winds, &mh.uwb, &mh.uwf)) || (rc = lev(H.winds, &mh.vwb, &mh.vwf)) ||
+        (rc = lev(H.currents, &mh.ucb, &mh.ucf)) || (rc = lev(H.currents, &mh.vcb, &mh.vcf)) ||
+        (rc = lev(H.air_density, &mh.rhoab, &mh.rhoaf)) || (rc = lev(H.water_density, &mh.rhowb, &mh.rhowf)) ||
+        (rc = lev(H.seaice, &mh.ficeb, &mh.ficef)))
+      return rc;
+    Member& d = hm[m];
+    d.off = mh.off; d.N = mh.N; d.ghost = mh.ghost; d.nmoff = mh.nmoff; d.NM = mh.NM; d.mm = H.mm; d.nm = H.nm;
+    d.iip = (H.iip >= 1 && H.iip <= H.im) ? mh.off + H.iip - 1 : -1;
+    d.dtamin = H.dtamin;
+    d.ctl = mh.ctl;
+    d.log = mh.log;
+    d.log_cap = mh.log_cap;
+    d.mi = mh.mi; d.ni = mh.ni;
+    d.uwb = mh.uwb; d.uwf = mh.uwf; d.vwb = mh.vwb; d.vwf = mh.vwf; d.ucb = mh.ucb; d.ucf = mh.ucf;
+    d.vcb = mh.vcb; d.vcf = mh.vcf; d.rhoab = mh.rhoab; d.rhoaf = mh.rhoaf; d.rhowb = mh.rhowb; d.rhowf = mh.rhowf;
+    d.ficeb = mh.ficeb; d.ficef = mh.ficef;
+    Ctl c{};
+    c.minphys_enc = enc_ord_h(std::numeric_limits<float>::infinity());
+    c.maxrot_enc = enc_ord_h(0.f);
+    c.first = 1;
+    c.zerocurrents = 1;
+    CU(cudaMemcpy(mh.ctl, &c, sizeof c, cudaMemcpyHostToDevice));
   }
-  const size_t n2 = (size_t)H.mm * H.nm;
-  auto lev = [&](bool on, float** b, float** f) -> int {
-    if (!on) return UMWM_OK;
-    CU(D.alloc(b, n2)); CU(D.alloc(f, n2));
-    return UMWM_OK;
-  };
-  if ((rc = lev(H.winds, &M.uwb, &M.uwf)) || (rc = lev(H.winds, &M.vwb, &M.vwf)) ||
-      (rc = lev(H.currents, &M.ucb, &M.ucf)) || (rc = lev(H.currents, &M.vcb, &M.vcf)) ||
-      (rc = lev(H.air_density, &M.rhoab, &M.rhoaf)) || (rc = lev(H.water_density, &M.rhowb, &M.rhowf)) ||
-      (rc = lev(H.seaice, &M.ficeb, &M.ficef)))
-    return rc;
-  P.uwb = M.uwb; P.uwf = M.uwf; P.vwb = M.vwb; P.vwf = M.vwf; P.ucb = M.ucb; P.ucf = M.ucf; P.vcb = M.vcb;
-  P.vcf = M.vcf; P.rhoab = M.rhoab; P.rhoaf = M.rhoaf; P.rhowb = M.rhowb; P.rhowf = M.rhowf; P.ficeb = M.ficeb;
-  P.ficef = M.ficef;
-  CU(D.alloc(&P.us, (size_t)std::max(1, H.lm) * ldN));
-  CU(D.alloc(&P.vs, (size_t)std::max(1, H.lm) * ldN));
-  CU(D.alloc(&P.ctl, 1));
-  P.log_cap = 1 << 20;
-  CU(D.alloc(&P.log, (size_t)P.log_cap * 8));
+  CU(D.alloc(&M.d_mem, M.mem.size()));
+  CU(cudaMemcpy(M.d_mem, hm.data(), hm.size() * sizeof(Member), cudaMemcpyHostToDevice));
+  {
+    std::vector<int> tm(p.ntiles, 0);
+    for (size_t m = 0; m < M.mem.size(); ++m)
+      for (int t = M.mem[m].off / TILE; t < (M.mem[m].off + M.mem[m].padded) / TILE; ++t) tm[t] = (int)m;
+    CU(D.alloc(&M.d_tile_mem, p.ntiles));
+    CU(cudaMemcpy(M.d_tile_mem, tm.data(), (size_t)p.ntiles * 4, cudaMemcpyHostToDevice));
+  }
+  p.mem = M.d_mem;
+  p.tile_mem = M.d_tile_mem;
 
-  // e = tiny(e), umwm_init.F90:1182 (spectrum and the ghost column of E*)
+  // e = tiny(e), umwm_init.F90:1182 (spectrum and the ghost points of E*)
   const float tiny = std::numeric_limits<float>::min();
   CU(launch_fill(M.E, spec, tiny, M.st));
   CU(launch_fill(M.ES, spec, tiny, M.st));
-  CU(launch_fill(M.EF, spec, 0.f, M.st));
-  // control block
-  Ctl c{};
-  c.minphys_enc = enc_ord_h(std::numeric_limits<float>::infinity());
-  c.maxrot_enc = enc_ord_h(0.f);
-  c.first = 1;
-  c.zerocurrents = 1;
-  CU(cudaMemcpy(P.ctl, &c, sizeof c, cudaMemcpyHostToDevice));
 
-  // input_nc(starttimestr), umwm_top.F90:25
-  M.readfile = H.winds || H.currents || H.air_density || H.water_density || H.seaice;
-  std::vector<float> uwf_h, vwf_h;
-  if ((rc = set_forcing_constants(M))) return rc;
-  if ((rc = read_forcing(M, time_key(H.starttimestr.c_str()), &uwf_h, &vwf_h))) return rc;
-  // init: first-guess drag and friction velocity, umwm_init.F90:1350-1365
-  std::vector<float> wspd(N + 1, H.wspd0);
-  if (H.winds)
-    for (int i = 1; i <= N; ++i) {
-      size_t q = H.i2(H.mi[i], H.ni[i]);
-      wspd[i] = std::sqrt(uwf_h[q] * uwf_h[q] + vwf_h[q] * vwf_h[q]);
-    }
+  // input_nc(starttimestr), umwm_top.F90:25, and init's first guess of the
+  // drag and friction velocity, umwm_init.F90:1350-1365
   std::vector<float> ust(ldN, 0.f), cd(ldN, 0.f);
-  for (int i = 1; i <= N; ++i) {
-    float c_ = 1.2e-3f;
-    if (wspd[i] > 11) c_ = (0.49f + 0.065f * wspd[i]) * 1e-3f;
-    cd[i - 1] = c_;
-    ust[i - 1] = std::sqrt(c_) * wspd[i];
+  for (MemberHost& mh : M.mem) {
+    const HostModel& H = mh.H;
+    std::vector<float> uwf_h, vwf_h;
+    if ((rc = set_forcing_constants(M, mh))) return rc;
+    if ((rc = read_forcing(M, mh, time_key(H.starttimestr.c_str()), &uwf_h, &vwf_h))) return rc;
+    std::vector<float> wspd(mh.N + 1, H.wspd0);
+    if (H.winds)
+      for (int i = 1; i <= mh.N; ++i) {
+        size_t q = H.i2(H.mi[i], H.ni[i]);
+        wspd[i] = std::sqrt(uwf_h[q] * uwf_h[q] + vwf_h[q] * vwf_h[q]);
+      }
+    for (int i = 1; i <= mh.N; ++i) {
+      float c_ = 1.2e-3f;
+      if (wspd[i] > 11) c_ = (0.49f + 0.065f * wspd[i]) * 1e-3f;
+      cd[mh.off + i - 1] = c_;
+      ust[mh.off + i - 1] = std::sqrt(c_) * wspd[i];
+    }
+    if (H.seaice) {  // init copies ficef into fice, umwm_init.F90:1351
+      std::vector<float> fi(mh.NM, 0.f);
+      const std::vector<float>& src = mh.in.forcing.find(time_key(H.starttimestr.c_str()))->second.at("fice");
+      for (int i = 1; i <= mh.NM; ++i) fi[i - 1] = src[H.i2(H.mi[i], H.ni[i])];
+      CU(cudaMemcpy(P.fice + mh.nmoff, fi.data(), (size_t)mh.NM * 4, cudaMemcpyHostToDevice));
+    }
   }
-  CU(cudaMemcpy(P.ustar, ust.data(), ldN * 4, cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(P.cd, cd.data(), ldN * 4, cudaMemcpyHostToDevice));
-  if (H.seaice) {
-    // init copies ficef into fice, umwm_init.F90:1351
-    std::vector<float> fi(NM, 0.f);
-    auto it = g_inputs.forcing.find(time_key(H.starttimestr.c_str()));
-    const std::vector<float>& src = it->second.at("fice");
-    for (int i = 1; i <= NM; ++i) fi[i - 1] = src[H.i2(H.mi[i], H.ni[i])];
-    CU(cudaMemcpy(P.fice, fi.data(), NM * 4, cudaMemcpyHostToDevice));
-  }
+  CU(cudaMemcpy(P.ustar, ust.data(), (size_t)ldN * 4, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(P.cd, cd.data(), (size_t)ldN * 4, cudaMemcpyHostToDevice));
   // stokes_drift('init'), umwm_top.F90:27
-  if (H.lm > 0) CU(launch_stokes(M.prm, P, M.st));
+  if (p.lm > 0) CU(launch_stokes(M.prm, P, M.st));
   CU(cudaStreamSynchronize(M.st));
   M.first = true;
-  M.firstdtg = !H.restart;
   M.on_device = true;
   return UMWM_OK;
 }
 
-int restart_read(Model& M, const std::string& key) {  // umwm_restart.F90:19-56
-  auto it = g_inputs.restarts.find(key);
-  if (it == g_inputs.restarts.end()) return fail(UMWM_ERR_INPUT, "restart_read: no restart staged for " + key);
-  const size_t nF = (size_t)M.prm.O * M.prm.P * M.prm.N;
-  if (it->second.first.size() != nF || it->second.second.size() != (size_t)M.prm.N)
+int set_state_member(Model& M, int m, const float* F, const float* ust) {
+  const Params& p = M.prm;
+  const MemberHost& mh = M.mem[m];
+  if (F) {
+    const size_t n = (size_t)p.O * p.P * mh.N;
+    float* tmp = nullptr;
+    CU(cudaMalloc(&tmp, n * 4));
+    cudaError_t e = cudaMemcpy(tmp, F, n * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_from_ref(p, tmp, M.E, mh.off, mh.N, M.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(M.st);
+    cudaFree(tmp);
+    CU(e);
+  }
+  if (ust) CU(cudaMemcpy(M.P.ustar + mh.off, ust, (size_t)mh.N * 4, cudaMemcpyHostToDevice));
+  return UMWM_OK;
+}
+
+int restart_read(Model& M, int m, const std::string& key) {  // umwm_restart.F90:19-56
+  MemberHost& mh = M.mem[m];
+  auto it = mh.in.restarts.find(key);
+  if (it == mh.in.restarts.end()) return fail(UMWM_ERR_INPUT, "restart_read: no restart staged for " + key);
+  const size_t nF = (size_t)M.prm.O * M.prm.P * mh.N;
+  if (it->second.first.size() != nF || it->second.second.size() != (size_t)mh.N)
     return fail(UMWM_ERR_INPUT, "restart_read: restart arrays have the wrong size");
-  return umwm_gpu_set_state(it->second.first.data(), it->second.second.data());
+  return set_state_member(M, m, it->second.first.data(), it->second.second.data());
 }
 
 int check_ctl(Model& M) {
-  Ctl c;
-  CU(cudaMemcpy(&c, M.P.ctl, sizeof c, cudaMemcpyDeviceToHost));
-  if (c.err) return fail(UMWM_ERR_TIMEOUT, "a device-side wait gave up");
+  std::vector<Ctl> c(M.mem.size());
+  CU(cudaMemcpy(c.data(), M.mem[0].ctl, c.size() * sizeof(Ctl), cudaMemcpyDeviceToHost));
+  for (auto& x : c)
+    if (x.err) return fail(UMWM_ERR_TIMEOUT, "a device-side wait gave up");
   return UMWM_OK;
 }
 
 int substep(Model& M) {
-  const int compute_rot = (M.H.currents || M.first) ? 1 : 0;
+  const int compute_rot = (M.prm.currents || M.first) ? 1 : 0;
   const Params& prm = M.prm;
   const Ptrs& P = M.P;
   const int first = M.first ? 1 : 0;
-  CU(timed(M, K_PREP, [&] { return launch_prep(prm, P, compute_rot, M.st); }));
+  CU(timed(M, K_PREP, [&] { return launch_prep(prm, P, compute_rot, M.max_nm, M.st); }));
   if (prm.ice_possible) CU(timed(M, K_SICE, [&] { return launch_sice(prm, P, M.st); }));
   CU(timed(M, K_PHYS, [&] { return launch_source_phys(prm, P, compute_rot, M.st); }));
   CU(timed(M, K_DTS, [&] { return launch_dts(prm, P, compute_rot, first, M.st); }));
@@ -452,17 +577,43 @@ int substep(Model& M) {
 }
 
 void print_screen(Model& M) {
+  MemberHost& mh = M.mem[0];
   int cnt = 0;
-  if (cudaMemcpy(&cnt, &M.P.ctl->log_count, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return;
-  if ((size_t)cnt <= M.screen_printed) return;
-  std::vector<double> rows((size_t)(cnt - M.screen_printed) * 8);
-  cudaMemcpy(rows.data(), M.P.log + M.screen_printed * 8, rows.size() * 8, cudaMemcpyDeviceToHost);
+  if (cudaMemcpy(&cnt, &mh.ctl->log_count, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return;
+  if ((size_t)cnt <= mh.screen_printed) return;
+  std::vector<double> rows((size_t)(cnt - mh.screen_printed) * 8);
+  cudaMemcpy(rows.data(), mh.log + mh.screen_printed * 8, rows.size() * 8, cudaMemcpyDeviceToHost);
   for (size_t r = 0; r < rows.size() / 8; ++r) {
     const double* L = &rows[r * 8];
     std::printf("  %4.2f  %8.3f %9.6f %9.6f %9.6f %9.6f %9.6f %9.6f\n", L[0], L[1], L[2], L[3], L[4], L[5], L[6], L[7]);
   }
-  M.screen_printed = cnt;
+  mh.screen_printed = cnt;
   std::fflush(stdout);
+}
+
+int member_substeps(Model& M, std::vector<int>& out) {
+  std::vector<Ctl> c(M.mem.size());
+  CU(cudaMemcpy(c.data(), M.mem[0].ctl, c.size() * sizeof(Ctl), cudaMemcpyDeviceToHost));
+  out.resize(c.size());
+  for (size_t m = 0; m < c.size(); ++m) out[m] = c[m].substep;
+  return UMWM_OK;
+}
+
+int finish_run(Model& M) {
+  CU(cudaEventRecord(M.ev1, M.st));
+  CU(cudaEventSynchronize(M.ev1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, M.ev0, M.ev1);
+  M.last_gpu_ms = ms;
+  std::vector<int> sub;
+  int rc = member_substeps(M, sub);
+  if (rc) return rc;
+  double bins = 0;
+  for (size_t m = 0; m < M.mem.size(); ++m)
+    bins += (double)(sub[m] - M.mem[m].substep_mark) * M.mem[m].N * M.prm.O * M.prm.P;
+  M.last_bins = bins;
+  collect_timings(M);
+  return check_ctl(M);
 }
 
 int run_impl(Model& M, const std::string& start, const std::string& stop) {
@@ -470,37 +621,33 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
   if (!time_from_string(start, t0) || !time_from_string(stop, t1))
     return fail(UMWM_ERR_ARG, "umwm_run: times must be 'YYYY-MM-DD hh:mm:ss'");
   int rc;
-  if (M.first && M.H.restart)
-    if ((rc = restart_read(M, time_key(start.c_str())))) return rc;
-  const long long sub0 = M.substeps;
+  if (M.first && M.prm.restart)
+    for (size_t m = 0; m < M.mem.size(); ++m)
+      if ((rc = restart_read(M, (int)m, time_key(start.c_str())))) return rc;
+  {
+    std::vector<int> sub;
+    if ((rc = member_substeps(M, sub))) return rc;
+    for (size_t m = 0; m < M.mem.size(); ++m) M.mem[m].substep_mark = sub[m];
+  }
   CU(cudaEventRecord(M.ev0, M.st));
   int64_t now = t0;
   while (now < t1) {
-    now += std::llround((double)M.H.dtg);
+    now += std::llround((double)M.prm.dtg);
     const std::string cur = time_to_string(now, '_');
     if (M.verbose) std::printf("umwm: solver: integrating to time: %s\n", cur.c_str());
-    if ((rc = forcing_input(M, cur))) return rc;
-    CU(cudaMemsetAsync(&M.P.ctl->sumt, 0, sizeof(float), M.st));
+    for (MemberHost& mh : M.mem)
+      if ((rc = forcing_input(M, mh, cur))) return rc;
+    CU(launch_begin_dtg(M.prm, M.st));  // sumt = 0, done = 0 for every member
     for (long long inner = 0;; ++inner) {
       if (inner > 10000000LL) return fail(UMWM_ERR_TIMEOUT, "umwm_run: more than 1e7 substeps in one dtg (dts stuck at 0?)");
-      if (M.max_substeps >= 0 && M.substeps >= M.max_substeps) {
-        CU(cudaEventRecord(M.ev1, M.st));
-        CU(cudaEventSynchronize(M.ev1));
-        float ms = 0;
-        cudaEventElapsedTime(&ms, M.ev0, M.ev1);
-        M.last_gpu_ms = ms;
-        M.last_bins = (double)(M.substeps - sub0) * M.prm.N * M.prm.O * M.prm.P;
-        collect_timings(M);
-        return check_ctl(M);
-      }
+      if (M.max_substeps >= 0 && M.substeps >= M.max_substeps) return finish_run(M);
       if ((rc = substep(M))) return rc;
-      CU(cudaMemcpyAsync(M.done_h, &M.P.ctl->done, sizeof(int), cudaMemcpyDeviceToHost, M.st));
+      CU(cudaMemcpyAsync(M.flag_h, &M.d_glob->not_done, sizeof(int), cudaMemcpyDeviceToHost, M.st));
       CU(cudaStreamSynchronize(M.st));
       collect_timings(M);
-      if (*M.done_h) break;
+      if (*M.flag_h == 0) break;
     }
-    M.firstdtg = false;
-    if (M.H.stokes && M.prm.lm > 0) {
+    if (M.mem[0].H.stokes && M.prm.lm > 0) {
       CU(timed(M, K_STOKES, [&] { return launch_stokes(M.prm, M.P, M.st); }));
       M.launches++;
     }
@@ -508,21 +655,19 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     M.launches++;
     if (M.verbose) print_screen(M);
   }
-  CU(cudaEventRecord(M.ev1, M.st));
-  CU(cudaEventSynchronize(M.ev1));
-  float ms = 0;
-  cudaEventElapsedTime(&ms, M.ev0, M.ev1);
-  M.last_gpu_ms = ms;
-  M.last_bins = (double)(M.substeps - sub0) * M.prm.N * M.prm.O * M.prm.P;
-  collect_timings(M);
-  return check_ctl(M);
+  return finish_run(M);
 }
 
-int init_common(const std::string& text, bool device) {
+int init_common(std::vector<Pending>& members, bool device) {
   g_model.reset();
   std::unique_ptr<Model> M(new Model());
-  if (!M->H.read_namelist(text)) return fail(UMWM_ERR_NAMELIST, M->H.err);
-  if (!M->H.build(g_inputs)) return fail(UMWM_ERR_INPUT, M->H.err);
+  M->mem.resize(members.size());
+  for (size_t m = 0; m < members.size(); ++m) {
+    MemberHost& mh = M->mem[m];
+    mh.in = std::move(members[m].in);
+    if (!mh.H.read_namelist(members[m].nml)) return fail(UMWM_ERR_NAMELIST, mh.H.err);
+    if (!mh.H.build(mh.in)) return fail(UMWM_ERR_INPUT, mh.H.err);
+  }
   if (device) {
     int rc = init_device(*M);
     if (rc) return rc;
@@ -530,6 +675,13 @@ int init_common(const std::string& text, bool device) {
   g_model = std::move(M);
   g_err.clear();
   return UMWM_OK;
+}
+
+int init_single(const std::string& text, bool device) {
+  std::vector<Pending> one(1);
+  one[0].nml = text;
+  one[0].in = g_inputs;  // staged inputs are kept for later initializations
+  return init_common(one, device);
 }
 
 Model* need_model(bool device) {
@@ -659,7 +811,7 @@ int umwm_gpu_clear_inputs(void) {
 
 int umwm_gpu_initialize_text(const char* text) {
   if (!text) return fail(UMWM_ERR_ARG, "initialize: null namelist");
-  return init_common(text, true);
+  return init_single(text, true);
 }
 
 int umwm_gpu_initialize(const char* path) {
@@ -668,12 +820,37 @@ int umwm_gpu_initialize(const char* path) {
   if (!f) return fail(UMWM_ERR_NAMELIST, "cannot open namelist " + p);
   std::stringstream ss;
   ss << f.rdbuf();
-  return init_common(ss.str(), true);
+  return init_single(ss.str(), true);
 }
 
 int umwm_gpu_setup_host(const char* text) {
   if (!text) return fail(UMWM_ERR_ARG, "setup_host: null namelist");
-  return init_common(text, false);
+  return init_single(text, false);
+}
+
+int umwm_gpu_ensemble_add(const char* nml_text) {
+  if (!nml_text) return fail(UMWM_ERR_ARG, "ensemble_add: null namelist");
+  Pending pm;
+  pm.nml = nml_text;
+  pm.in = std::move(g_inputs);
+  g_inputs = Inputs();
+  g_pending.push_back(std::move(pm));
+  return UMWM_OK;
+}
+
+int umwm_gpu_ensemble_initialize(void) {
+  if (g_pending.empty()) return fail(UMWM_ERR_STATE, "ensemble_initialize: no member added");
+  std::vector<Pending> members = std::move(g_pending);
+  g_pending.clear();
+  return init_common(members, true);
+}
+
+int umwm_gpu_select_member(int m) {
+  Model* M = need_model(false);
+  if (!M) return UMWM_ERR_STATE;
+  if (m < 0 || m >= (int)M->mem.size()) return fail(UMWM_ERR_ARG, "select_member: no such member");
+  M->sel = m;
+  return UMWM_OK;
 }
 
 int umwm_gpu_run(const char* start, const char* stop) {
@@ -692,7 +869,7 @@ int umwm_gpu_get_dims(int* dims) {
   Model* M = need_model(false);
   if (!M) return UMWM_ERR_STATE;
   if (!dims) return fail(UMWM_ERR_ARG, "get_dims: null");
-  const HostModel& H = M->H;
+  const HostModel& H = M->mem[M->sel].H;
   int v[8] = {H.mm, H.nm, H.om, H.pm, H.im, H.imm, H.lm, (int)M->substeps};
   std::memcpy(dims, v, sizeof v);
   return UMWM_OK;
@@ -701,37 +878,26 @@ int umwm_gpu_get_dims(int* dims) {
 int umwm_gpu_set_state(const float* F, const float* ust) {
   Model* M = need_model(true);
   if (!M) return UMWM_ERR_STATE;
-  const Params& p = M->prm;
-  if (F) {
-    const size_t n = (size_t)p.O * p.P * p.N;
-    float* tmp = nullptr;
-    CU(cudaMalloc(&tmp, n * 4));
-    cudaError_t e = cudaMemcpy(tmp, F, n * 4, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = launch_from_ref(p, tmp, M->E, M->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(M->st);
-    cudaFree(tmp);
-    CU(e);
-  }
-  if (ust) CU(cudaMemcpy(M->P.ustar, ust, (size_t)p.N * 4, cudaMemcpyHostToDevice));
-  return UMWM_OK;
+  return set_state_member(*M, M->sel, F, ust);
 }
 
 int umwm_gpu_get_state(float* F, float* ust) {
   Model* M = need_model(true);
   if (!M) return UMWM_ERR_STATE;
   const Params& p = M->prm;
+  const MemberHost& mh = M->mem[M->sel];
   CU(cudaStreamSynchronize(M->st));
   if (F) {
-    const size_t n = (size_t)p.O * p.P * p.N;
+    const size_t n = (size_t)p.O * p.P * mh.N;
     float* tmp = nullptr;
     CU(cudaMalloc(&tmp, n * 4));
-    cudaError_t e = launch_to_ref(p, M->E, tmp, M->st);
+    cudaError_t e = launch_to_ref(p, M->E, tmp, mh.off, mh.N, M->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(M->st);
     if (e == cudaSuccess) e = cudaMemcpy(F, tmp, n * 4, cudaMemcpyDeviceToHost);
     cudaFree(tmp);
     CU(e);
   }
-  if (ust) CU(cudaMemcpy(ust, M->P.ustar, (size_t)p.N * 4, cudaMemcpyDeviceToHost));
+  if (ust) CU(cudaMemcpy(ust, M->P.ustar + mh.off, (size_t)mh.N * 4, cudaMemcpyDeviceToHost));
   return UMWM_OK;
 }
 
@@ -743,6 +909,7 @@ int umwm_gpu_get_state_noalloc(float* F, float* ust) {
   Model* M = need_model(true);
   if (!M) return UMWM_ERR_STATE;
   const Params& p = M->prm;
+  const MemberHost& mh = M->mem[M->sel];
   const size_t R = (size_t)p.O * p.P;
   if (R > NOALLOC_SCRATCH_FLOATS)
     return fail(UMWM_ERR_ARG, "get_state_noalloc: one point's spectrum (om*pm floats) exceeds the 16 MiB scratch");
@@ -752,16 +919,16 @@ int umwm_gpu_get_state_noalloc(float* F, float* ust) {
   CU(cudaStreamSynchronize(M->st));
   if (F) {
     const int chunk = (int)(NOALLOC_SCRATCH_FLOATS / R);
-    for (int j0 = 0; j0 < p.N; j0 += chunk) {
-      const int nj = std::min(chunk, p.N - j0);
+    for (int j0 = 0; j0 < mh.N; j0 += chunk) {
+      const int nj = std::min(chunk, mh.N - j0);
       dim3 grid((unsigned)((R + 31) / 32), (unsigned)((nj + 31) / 32)), block(32, 8);
-      k_to_ref_chunk<<<grid, block, 0, M->st>>>(p, M->E, scratch, j0, nj);
+      k_to_ref_chunk<<<grid, block, 0, M->st>>>(p, M->E, scratch, mh.off + j0, nj);
       CU(cudaGetLastError());
       CU(cudaMemcpyAsync(F + (size_t)j0 * R, scratch, (size_t)nj * R * sizeof(float), cudaMemcpyDeviceToHost, M->st));
       CU(cudaStreamSynchronize(M->st));
     }
   }
-  if (ust) CU(cudaMemcpy(ust, M->P.ustar, (size_t)p.N * 4, cudaMemcpyDeviceToHost));
+  if (ust) CU(cudaMemcpy(ust, M->P.ustar + mh.off, (size_t)mh.N * 4, cudaMemcpyDeviceToHost));
   return UMWM_OK;
 }
 
@@ -769,7 +936,8 @@ int umwm_gpu_get_field(const char* name, float* out, long n) {
   Model* M = need_model(false);
   if (!M) return UMWM_ERR_STATE;
   if (!name || !out) return fail(UMWM_ERR_ARG, "get_field: null argument");
-  const HostModel& H = M->H;
+  const MemberHost& mh = M->mem[M->sel];
+  const HostModel& H = mh.H;
   const std::string s(name);
   const int N = H.im, NM = H.imm, O = H.om;
   auto need = [&](long k) { return n >= k ? UMWM_OK : fail(UMWM_ERR_ARG, "get_field: buffer too small for " + s); };
@@ -848,7 +1016,7 @@ int umwm_gpu_get_field(const char* name, float* out, long n) {
   for (size_t q = 0; q < sizeof(wetnames) / sizeof(wetnames[0]); ++q)
     if (s == wetnames[q]) {
       if (need(N)) return UMWM_ERR_ARG;
-      CU(cudaMemcpy(out, wetptrs[q], (size_t)N * 4, cudaMemcpyDeviceToHost));
+      CU(cudaMemcpy(out, wetptrs[q] + mh.off, (size_t)N * 4, cudaMemcpyDeviceToHost));
       return UMWM_OK;
     }
   static const char* allnames[] = {"wspd", "wdir", "uc", "vc", "rhoa", "rhow", "rhorat", "fice"};
@@ -856,18 +1024,19 @@ int umwm_gpu_get_field(const char* name, float* out, long n) {
   for (size_t q = 0; q < 8; ++q)
     if (s == allnames[q]) {
       if (need(NM)) return UMWM_ERR_ARG;
-      CU(cudaMemcpy(out, allptrs[q], (size_t)NM * 4, cudaMemcpyDeviceToHost));
+      CU(cudaMemcpy(out, allptrs[q] + mh.nmoff, (size_t)NM * 4, cudaMemcpyDeviceToHost));
       return UMWM_OK;
     }
   if (s == "us" || s == "vs") {
     if (need((long)H.lm * N)) return UMWM_ERR_ARG;
     const float* src = s == "us" ? P.us : P.vs;
     for (int l = 0; l < H.lm; ++l)
-      CU(cudaMemcpy(out + (size_t)l * N, src + (size_t)l * M->prm.ldN, (size_t)N * 4, cudaMemcpyDeviceToHost));
+      CU(cudaMemcpy(out + (size_t)l * N, src + (size_t)l * M->prm.ldN + mh.off, (size_t)N * 4,
+                    cudaMemcpyDeviceToHost));
     return UMWM_OK;
   }
   Ctl c;
-  CU(cudaMemcpy(&c, P.ctl, sizeof c, cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(&c, mh.ctl, sizeof c, cudaMemcpyDeviceToHost));
   if (s == "dts") return scalar(c.dts);
   if (s == "dta") return scalar(c.dta);
   if (s == "dtr") return scalar(c.dtr);
@@ -880,7 +1049,8 @@ int umwm_gpu_get_field_i(const char* name, int* out, long n) {
   Model* M = need_model(false);
   if (!M) return UMWM_ERR_STATE;
   if (!name || !out) return fail(UMWM_ERR_ARG, "get_field_i: null argument");
-  const HostModel& H = M->H;
+  const MemberHost& mh = M->mem[M->sel];
+  const HostModel& H = mh.H;
   const std::string s(name);
   auto vec = [&](const std::vector<int>& v, int lo, int hi) {
     if (n < hi - lo + 1) return fail(UMWM_ERR_ARG, "get_field_i: buffer too small for " + s);
@@ -903,15 +1073,22 @@ int umwm_gpu_get_field_i(const char* name, int* out, long n) {
   if (s == "iie") return vec(H.iie, 1, H.imm);
   if (s == "iis") return vec(H.iis, 1, H.imm);
   if (s == "iin") return vec(H.iin, 1, H.imm);
-  if (s == "im" || s == "imm" || s == "iip") {
+  if (s == "im" || s == "imm" || s == "iip" || s == "members") {
     if (n < 1) return fail(UMWM_ERR_ARG, "get_field_i: buffer too small");
-    out[0] = s == "im" ? H.im : s == "imm" ? H.imm : H.iip;
+    out[0] = s == "im" ? H.im : s == "imm" ? H.imm : s == "iip" ? H.iip : (int)M->mem.size();
     return UMWM_OK;
   }
   if (s == "oc") {
     if (!M->on_device) return fail(UMWM_ERR_STATE, "get_field_i: oc needs the device model");
     if (n < H.im) return fail(UMWM_ERR_ARG, "get_field_i: buffer too small");
-    CU(cudaMemcpy(out, M->P.oc, (size_t)H.im * 4, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(out, M->P.oc + mh.off, (size_t)H.im * 4, cudaMemcpyDeviceToHost));
+    return UMWM_OK;
+  }
+  if (s == "substeps") {
+    if (!M->on_device || n < 1) return fail(UMWM_ERR_STATE, "get_field_i: substeps needs the device model");
+    Ctl c;
+    CU(cudaMemcpy(&c, mh.ctl, sizeof c, cudaMemcpyDeviceToHost));
+    out[0] = c.substep;
     return UMWM_OK;
   }
   return fail(UMWM_ERR_ARG, "get_field_i: unknown field " + s);
@@ -920,12 +1097,13 @@ int umwm_gpu_get_field_i(const char* name, int* out, long n) {
 int umwm_gpu_get_screen(double* out, long n, long* rows) {
   Model* M = need_model(true);
   if (!M) return UMWM_ERR_STATE;
+  const MemberHost& mh = M->mem[M->sel];
   int cnt = 0;
-  CU(cudaMemcpy(&cnt, &M->P.ctl->log_count, 4, cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(&cnt, &mh.ctl->log_count, 4, cudaMemcpyDeviceToHost));
   if (rows) *rows = cnt;
   if (out && n > 0) {
     long k = std::min<long>(n / 8, cnt);
-    CU(cudaMemcpy(out, M->P.log, (size_t)k * 8 * sizeof(double), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(out, mh.log, (size_t)k * 8 * sizeof(double), cudaMemcpyDeviceToHost));
   }
   return UMWM_OK;
 }

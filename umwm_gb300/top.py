@@ -78,6 +78,21 @@ def umwm_finalize():
     check(lib().umwm_gpu_finalize())
 
 
+def ensemble_add(nml_text):
+    """Add an ensemble member: this namelist plus the inputs staged so far."""
+    check(lib().umwm_gpu_ensemble_add(nml_text.encode()))
+
+
+def ensemble_initialize():
+    """umwm_initialize for every added member, as one model."""
+    check(lib().umwm_gpu_ensemble_initialize())
+
+
+def select_member(m):
+    """Member that get_field / get_state / set_state act on."""
+    check(lib().umwm_gpu_select_member(int(m)))
+
+
 def setup_host(nml_text):
     """Host part of umwm_initialize only (no GPU needed)."""
     check(lib().umwm_gpu_setup_host(nml_text.encode()))
