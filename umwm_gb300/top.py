@@ -166,7 +166,7 @@ def get_field_i(name):
         out = np.zeros(d["mm"] * d["nm"], dtype=np.int32)
         check(lib().umwm_gpu_get_field_i(name.encode(), out.ctypes.data_as(_ip), out.size))
         return out.reshape(d["nm"], d["mm"]).T
-    if name in ("im", "imm", "iip"):
+    if name in ("im", "imm", "iip", "members", "substeps"):
         out = np.zeros(1, dtype=np.int32)
         check(lib().umwm_gpu_get_field_i(name.encode(), out.ctypes.data_as(_ip), 1))
         return int(out[0])
