@@ -152,9 +152,15 @@ int umwm_gpu_get_field_i(const char* name, int* out, long n);
 int umwm_gpu_get_screen(double* out, long n, long* rows);
 
 /* Options: "verbose" (print the screen lines), "max_substeps" (stop a run
- * after that many substeps in total; -1 = off), "check_finite" (finite
- * check of the state after each outer step), "use_graph" (run the inner
- * loop as one CUDA graph with a device-side while node). */
+ * after that many substeps in total; -1 = off), "check_finite" (after each
+ * outer step, check that the significant wave height and friction velocity
+ * of every wet point are finite -- a NaN/Inf bin makes its point's wave
+ * height non-finite -- and fail with UMWM_ERR_NONFINITE otherwise),
+ * "use_graph" (run the inner loop as a CUDA graph with a device-side while
+ * node: one host synchronisation per outer step instead of one per
+ * substep; results are bit-identical), "kernel_timing" (CUDA-event time of
+ * each kernel, read with umwm_gpu_get_stat "ms:<kernel>"; the inner loop
+ * then runs host-driven), "device" (CUDA device of the next initialize). */
 int umwm_gpu_set_option(const char* name, double value);
 
 /* Run statistics: "substeps", "gpu_ms" (device time of the last run),

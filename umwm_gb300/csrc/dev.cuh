@@ -94,6 +94,9 @@ struct Member {
 // control shared by all members (one per model)
 struct Global {
   int not_done;            // members still inside the current dtg after this substep
+  int budget;              // substeps the graph-driven inner loop may still run (-1: no limit)
+  int iters;               // substeps the graph-driven inner loop ran since it was armed
+  int nonfinite;           // non-finite values found by the last finite check
 };
 
 struct Ptrs {

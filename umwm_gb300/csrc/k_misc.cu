@@ -314,6 +314,29 @@ __global__ void k_begin_dtg(const Params prm) {
   }
 }
 
+// Graph-driven inner loop: arm before the graph launch, then after each
+// substep count it and set the while node's condition (another substep while
+// a member is inside the dtg and the budget lasts).
+__global__ void k_loop_arm(Global* g, int budget) {
+  g->budget = budget;
+  g->iters = 0;
+}
+
+__global__ void k_loop_cond(Global* g, cudaGraphConditionalHandle h) {
+  g->iters += 1;
+  if (g->budget > 0) g->budget -= 1;
+  cudaGraphSetConditional(h, (g->not_done && g->budget != 0) ? 1u : 0u);
+}
+
+// Count the NaN/Inf values of a[0..n) into *count (option "check_finite").
+__global__ void k_count_nonfinite(const float* __restrict__ a, size_t n, int* count) {
+  int bad = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    bad += isfinite(a[i]) ? 0 : 1;
+  bad = __syncthreads_count(bad > 0);
+  if (threadIdx.x == 0 && bad) atomicAdd(count, bad);
+}
+
 __global__ void k_fill(float* a, size_t n, float v) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) a[i] = v;
 }
@@ -361,6 +384,18 @@ cudaError_t launch_from_ref(const Params& prm, const float* F, float* E, int off
 }
 cudaError_t launch_begin_dtg(const Params& prm, cudaStream_t st) {
   k_begin_dtg<<<1, 256, 0, st>>>(prm);
+  return cudaGetLastError();
+}
+cudaError_t launch_loop_arm(Global* g, int budget, cudaStream_t st) {
+  k_loop_arm<<<1, 1, 0, st>>>(g, budget);
+  return cudaGetLastError();
+}
+cudaError_t launch_loop_cond(Global* g, cudaGraphConditionalHandle h, cudaStream_t st) {
+  k_loop_cond<<<1, 1, 0, st>>>(g, h);
+  return cudaGetLastError();
+}
+cudaError_t launch_count_nonfinite(const float* a, size_t n, int* count, cudaStream_t st) {
+  k_count_nonfinite<<<grid_for((long)std::min<size_t>(n, 1u << 30), 256), 256, 0, st>>>(a, n, count);
   return cudaGetLastError();
 }
 cudaError_t launch_fill(float* a, size_t n, float v, cudaStream_t st) {

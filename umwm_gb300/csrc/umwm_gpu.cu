@@ -96,7 +96,9 @@ struct Model {
   Global* d_glob = nullptr;
   cudaStream_t st = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  int* flag_h = nullptr;  // pinned read-back of Global::not_done
+  Global* flag_h = nullptr;  // pinned read-back of the Global block
+  cudaGraph_t graph = nullptr;          // inner loop as a while node (option "use_graph")
+  cudaGraphExec_t graph_exec = nullptr;
   bool first = true;
   long long substeps = 0, max_substeps = -1;
   bool verbose = false, check_finite = false, use_graph = false;
@@ -118,6 +120,8 @@ struct Model {
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (flag_h) cudaFreeHost(flag_h);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
   }
 };
 
@@ -347,7 +351,7 @@ int init_device(Model& M) {
   CU(cudaStreamCreateWithFlags(&M.st, cudaStreamNonBlocking));
   CU(cudaEventCreate(&M.ev0));
   CU(cudaEventCreate(&M.ev1));
-  CU(cudaMallocHost(&M.flag_h, sizeof(int)));
+  CU(cudaMallocHost(&M.flag_h, sizeof(Global)));
   Ptrs& P = M.P;
   CU(D.alloc(&M.E, spec, false));
   CU(D.alloc(&M.ES, spec, false));
@@ -553,28 +557,71 @@ int check_ctl(Model& M) {
   return UMWM_OK;
 }
 
-int substep(Model& M) {
-  const int compute_rot = (M.prm.currents || M.first) ? 1 : 0;
+// Enqueue the launches of one substep: prep, [sice], phys, dts, integ,
+// advect, [diag on the first substep of a run], screen.
+int enqueue_substep(Model& M, int compute_rot, int first, bool diag) {
   const Params& prm = M.prm;
   const Ptrs& P = M.P;
-  const int first = M.first ? 1 : 0;
   CU(timed(M, K_PREP, [&] { return launch_prep(prm, P, compute_rot, M.max_nm, M.st); }));
   if (prm.ice_possible) CU(timed(M, K_SICE, [&] { return launch_sice(prm, P, M.st); }));
   CU(timed(M, K_PHYS, [&] { return launch_source_phys(prm, P, compute_rot, M.st); }));
   CU(timed(M, K_DTS, [&] { return launch_dts(prm, P, compute_rot, first, M.st); }));
   CU(timed(M, K_INTEG, [&] { return launch_source_integ(prm, P, M.st); }));
   CU(timed(M, K_ADVECT, [&] { return launch_advect(prm, P, M.st); }));
-  M.launches += 5 + (prm.ice_possible ? 1 : 0);
-  if (M.first) {
-    CU(timed(M, K_DIAG, [&] { return launch_diag(prm, P, M.st); }));
-    M.launches++;
-    M.first = false;
-  }
+  if (diag) CU(timed(M, K_DIAG, [&] { return launch_diag(prm, P, M.st); }));
   CU(timed(M, K_SCREEN, [&] { return launch_screen(prm, P, M.st); }));
-  M.launches++;
+  return UMWM_OK;
+}
+
+int substep_launches(const Model& M, bool diag) { return 6 + (M.prm.ice_possible ? 1 : 0) + (diag ? 1 : 0); }
+
+int substep(Model& M) {
+  const bool first = M.first;
+  int rc = enqueue_substep(M, (M.prm.currents || first) ? 1 : 0, first ? 1 : 0, first);
+  if (rc) return rc;
+  M.launches += substep_launches(M, first);
+  M.first = false;
   M.substeps++;
   return UMWM_OK;
 }
+
+// The inner loop of umwm_run as a CUDA graph: one while node whose body is a
+// substep (after the first of a run: compute_rot = currents, first = 0)
+// followed by k_loop_cond, which keeps the loop going while a member is
+// inside the dtg and the armed budget lasts.  Launch parameters are fixed
+// after initialize (forcing updates are device copies into fixed buffers), so
+// the graph is built once per model.
+int build_graph(Model& M) {
+  if (M.graph_exec) return UMWM_OK;
+  CU(cudaGraphCreate(&M.graph, 0));
+  cudaGraphConditionalHandle h;
+  CU(cudaGraphConditionalHandleCreate(&h, M.graph, 1u, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp{};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CU(cudaGraphAddNode(&node, M.graph, nullptr, nullptr, 0, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CU(cudaStreamBeginCaptureToGraph(M.st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  const bool kt = M.ktime;
+  M.ktime = false;
+  int rc = enqueue_substep(M, M.prm.currents ? 1 : 0, 0, false);
+  cudaError_t e = rc ? cudaSuccess : launch_loop_cond(M.d_glob, h, M.st);
+  M.ktime = kt;
+  cudaGraph_t captured = nullptr;
+  cudaError_t ec = cudaStreamEndCapture(M.st, &captured);
+  if (rc) return rc;
+  CU(e);
+  CU(ec);
+  CU(cudaGraphInstantiate(&M.graph_exec, M.graph, 0));
+  return UMWM_OK;
+}
+
+// Substeps one graph launch may run before control returns to the host,
+// which then relaunches it (bounded device-side loop).
+constexpr int GRAPH_CHUNK = 4096;
 
 void print_screen(Model& M) {
   MemberHost& mh = M.mem[0];
@@ -638,14 +685,30 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     for (MemberHost& mh : M.mem)
       if ((rc = forcing_input(M, mh, cur))) return rc;
     CU(launch_begin_dtg(M.prm, M.st));  // sumt = 0, done = 0 for every member
-    for (long long inner = 0;; ++inner) {
+    for (long long inner = 0;;) {
       if (inner > 10000000LL) return fail(UMWM_ERR_TIMEOUT, "umwm_run: more than 1e7 substeps in one dtg (dts stuck at 0?)");
       if (M.max_substeps >= 0 && M.substeps >= M.max_substeps) return finish_run(M);
+      if (M.use_graph && !M.first && !M.ktime) {
+        if ((rc = build_graph(M))) return rc;
+        long long budget = GRAPH_CHUNK;
+        if (M.max_substeps >= 0) budget = std::min(budget, M.max_substeps - M.substeps);
+        CU(launch_loop_arm(M.d_glob, (int)budget, M.st));
+        CU(cudaGraphLaunch(M.graph_exec, M.st));
+        CU(cudaMemcpyAsync(M.flag_h, M.d_glob, sizeof(Global), cudaMemcpyDeviceToHost, M.st));
+        CU(cudaStreamSynchronize(M.st));
+        const int it = M.flag_h->iters;
+        M.substeps += it;
+        M.launches += 1 + (long long)it * (substep_launches(M, false) + 1);
+        inner += it;
+        if (M.flag_h->not_done == 0) break;
+        continue;
+      }
       if ((rc = substep(M))) return rc;
-      CU(cudaMemcpyAsync(M.flag_h, &M.d_glob->not_done, sizeof(int), cudaMemcpyDeviceToHost, M.st));
+      ++inner;
+      CU(cudaMemcpyAsync(M.flag_h, M.d_glob, sizeof(Global), cudaMemcpyDeviceToHost, M.st));
       CU(cudaStreamSynchronize(M.st));
       collect_timings(M);
-      if (*M.flag_h == 0) break;
+      if (M.flag_h->not_done == 0) break;
     }
     if (M.mem[0].H.stokes && M.prm.lm > 0) {
       CU(timed(M, K_STOKES, [&] { return launch_stokes(M.prm, M.P, M.st); }));
@@ -654,6 +717,18 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     CU(timed(M, K_DIAG, [&] { return launch_diag(M.prm, M.P, M.st); }));
     M.launches++;
     if (M.verbose) print_screen(M);
+    if (M.check_finite) {
+      // a NaN/Inf bin makes its point's significant wave height non-finite
+      CU(cudaMemsetAsync(&M.d_glob->nonfinite, 0, sizeof(int), M.st));
+      CU(launch_count_nonfinite(M.P.ht, (size_t)M.prm.ldN, &M.d_glob->nonfinite, M.st));
+      CU(launch_count_nonfinite(M.P.ustar, (size_t)M.prm.ldN, &M.d_glob->nonfinite, M.st));
+      M.launches += 2;
+      CU(cudaMemcpyAsync(M.flag_h, M.d_glob, sizeof(Global), cudaMemcpyDeviceToHost, M.st));
+      CU(cudaStreamSynchronize(M.st));
+      if (M.flag_h->nonfinite)
+        return fail(UMWM_ERR_NONFINITE, "umwm_run: non-finite significant wave height or friction velocity after "
+                                        "the step to " + cur);
+    }
   }
   return finish_run(M);
 }
