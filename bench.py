@@ -225,6 +225,92 @@ def run_reference(args):
     return 0
 
 
+def run_ensemble(args):
+    """Batched ensemble against sequential plain runs: n hurricane members
+    (grid sizes uniform in [200x200, 1000x600], Vmax/Rmax/heading scaled by
+    seeded factors in [0.85, 1.15]), cold start.  Each arm runs a first dtg
+    untimed (the calm first substep, graph instantiation) and times the
+    second: the sequential arm member by member (initialize untimed), the
+    batched arm as one ensemble.  Both arms run the graph-driven inner loop.
+    The significant wave height of every member after the timed dtg must be
+    bit-identical between the arms."""
+    rank, world, local_rank = rank_info()
+    import umwm_gb300 as U
+    from umwm_gb300 import configs
+
+    dtg = 600
+    members = configs.ensemble_members(args.members, seed=11, hours=2 * dtg / 3600.0, dtg=dtg, warm=False)
+    start = members[0].start
+    mid = configs._time_str(start, dtg)
+    stop = members[0].stop
+    U.set_option("device", local_rank)
+    wet = [c.meta["im"] for c in members]
+
+    seq_ms = seq_bins = seq_sub = 0.0
+    seq_ht = []
+    t_seq = time.perf_counter()
+    for c in members:
+        U.clear_inputs()
+        c.stage(U)
+        U.umwm_initialize(nml_text=c.nml)
+        U.set_option("use_graph", 1)
+        U.umwm_run(start, mid)
+        s0 = U.dims()["substeps"]
+        U.umwm_run(mid, stop)
+        seq_ms += U.stat("gpu_ms")
+        seq_bins += U.stat("bin_updates")
+        seq_sub += U.dims()["substeps"] - s0
+        seq_ht.append(U.get_field("ht"))
+        U.umwm_finalize()
+    t_seq = time.perf_counter() - t_seq
+
+    U.clear_inputs()
+    for c in members:
+        c.stage(U)
+        U.ensemble_add(c.nml)
+    t0 = time.perf_counter()
+    U.ensemble_initialize()
+    t_init = time.perf_counter() - t0
+    U.set_option("use_graph", 1)
+    U.umwm_run(start, mid)
+    launches0 = U.stat("launches")
+    clocks = Clocks(local_rank)
+    clocks.start()
+    s0 = U.dims()["substeps"]
+    U.umwm_run(mid, stop)
+    clk = clocks.stop()
+    bat_ms = U.stat("gpu_ms")
+    bat_bins = U.stat("bin_updates")
+    bat_outer = U.dims()["substeps"] - s0
+    launches = int(U.stat("launches") - launches0)
+    same = True
+    for m in range(len(members)):
+        U.select_member(m)
+        same = same and bool(np.array_equal(U.get_field("ht"), seq_ht[m]))
+    U.umwm_finalize()
+
+    batched = bat_bins / (bat_ms / 1e3)
+    sequential = seq_bins / (seq_ms / 1e3)
+    line = {"metric": METRIC, "value": batched, "unit": UNIT, "n_gpus": 1, "steps": bat_outer,
+            "warmup": 1, "ms_per_step": bat_ms / max(bat_outer, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "ensemble of %d hurricane members, grid sizes uniform in [200x200, 1000x600] "
+                                   "(seed 11), Vmax/Rmax/heading x U(0.85, 1.15), cold start, dtg %d s: the second "
+                                   "dtg timed" % (len(members), dtg),
+                       "members": len(members), "wet_points": int(sum(wet)), "wet_min": int(min(wet)),
+                       "wet_max": int(max(wet)), "bins_per_point": BINS},
+            "batched": {"value": batched, "gpu_ms": bat_ms, "bin_updates": bat_bins, "init_s": t_init},
+            "sequential": {"value": sequential, "gpu_ms": seq_ms, "bin_updates": seq_bins,
+                           "member_substeps": seq_sub, "wall_s_incl_init": t_seq},
+            "batched_over_sequential": batched / sequential,
+            "bins_match": bool(bat_bins == seq_bins), "hs_bit_identical": same,
+            "gpu_launches": launches, "clocks": clk,
+            "timing": "CUDA events on the model's stream around umwm_gpu_run of the second dtg (both arms)"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -236,11 +322,15 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="random_field", choices=["random_field", "ensemble"])
+    ap.add_argument("--members", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "ensemble":
+        return run_ensemble(args)
 
     rank, world, local_rank = rank_info()
     dist = Dist(world, local_rank)

@@ -49,7 +49,7 @@ def test_graph_loop_matches_host_loop(lib_built, max_substeps):
     from umwm_gb300 import configs
 
     U = lib_built
-    case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0, dtg=600)
+    case = configs.random_field(mm=48, nm=40, hours=2, dx=2000.0)
     host = _run(U, case, False, max_substeps)
     graph = _run(U, case, True, max_substeps)
     _same(host, graph)

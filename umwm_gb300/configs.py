@@ -228,8 +228,10 @@ def holland_wind(X, Y, xc, yc, vmax=50.0, rmax=30e3, B=1.5, heading=0.0, vt=5.0,
 
 
 def hurricane(mm=800, nm=800, hours=12, dx=2000.0, seed=3, dtg=600, vmax=50.0, rmax=30e3, B=1.5, hs=0.2, fp=0.3,
-              **nml):
-    """Translating Holland vortex over a linear shelf."""
+              heading_scale=1.0, warm=True, **nml):
+    """Translating Holland vortex over a linear shelf.  heading_scale scales
+    the seeded heading (ensemble perturbations); warm=False starts cold
+    (restart=.false.: the model's own initial spectrum, no restart staged)."""
     rng = np.random.Generator(np.random.Philox(seed))
     x = (np.arange(mm) * dx)[:, None] * np.ones((1, nm))
     y = (np.arange(nm) * dx)[None, :] * np.ones((mm, 1))
@@ -238,7 +240,7 @@ def hurricane(mm=800, nm=800, hours=12, dx=2000.0, seed=3, dtg=600, vmax=50.0, r
     rough = smooth_field((mm, nm), 5.0, rng)
     depth = depth * (1 + 0.05 * np.clip(rough / 3.0, -1, 1))
     z = (-depth).astype(np.float32)
-    heading = rng.uniform(0, 2 * np.pi)
+    heading = rng.uniform(0, 2 * np.pi) * heading_scale
     cur_dir = rng.uniform(0, 2 * np.pi)
     vt = 5.0
     Lx, Ly = mm * dx, nm * dx
@@ -259,17 +261,36 @@ def hurricane(mm=800, nm=800, hours=12, dx=2000.0, seed=3, dtg=600, vmax=50.0, r
         forcing[_time_str(start, t)] = {"uw": uw, "vw": vw, "uc": ucf, "vc": vcf}
     mask = sea_mask_from_z(z)
     wm, wn = unroll(mask)
-    kw = dict(mm=mm, nm=nm, delx=dx, dely=dx, topoFromFile=True, winds=True, currents=True, restart=True,
+    kw = dict(mm=mm, nm=nm, delx=dx, dely=dx, topoFromFile=True, winds=True, currents=True, restart=warm,
               startTimeStr=start, stopTimeStr=stop, xpl=mm // 2, ypl=nm // 2, dtg=dtg)
     kw.update(nml)
     text = make_namelist(**kw)
+    meta = dict(mm=mm, nm=nm, hours=hours, im=len(wm), heading=heading, vmax=vmax, rmax=rmax)
+    if not warm:
+        return Case("hurricane_%dx%d" % (mm, nm), text, start, stop, gridtopo={"z": z}, forcing=forcing, meta=meta)
     f0 = forcing[start]
     wdir = np.arctan2(f0["vw"][wm - 1, wn - 1], f0["uw"][wm - 1, wn - 1]).astype(np.float64)
     F = jonswap_state(depth[wm - 1, wn - 1], wdir, hs, fp, om=kw.get("om", 37), pm=kw.get("pm", 36), seed=seed + 100)
     ust = _ustar_guess(np.hypot(f0["uw"], f0["vw"])[wm - 1, wn - 1])
     return Case("hurricane_%dx%d" % (mm, nm), text, start, stop, gridtopo={"z": z}, forcing=forcing,
-                restart=(start, F, ust), meta=dict(mm=mm, nm=nm, hours=hours, im=len(wm), heading=heading))
+                restart=(start, F, ust), meta=meta)
 
 
-__all__ = ["Case", "fetch_limited", "random_field", "hurricane", "jonswap_state", "unroll", "sea_mask_from_z",
+def ensemble_members(n=64, seed=11, size_lo=(200, 200), size_hi=(1000, 600), hours=12, dx=2000.0, dtg=600,
+                     warm=True, **kw):
+    """n hurricane members: grid sizes uniform in [size_lo, size_hi] and Vmax,
+    Rmax and heading scaled by seeded factors in [0.85, 1.15]; member m uses
+    seed + m for its bathymetry roughness and base heading."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    out = []
+    for m in range(n):
+        mm = int(rng.integers(size_lo[0], size_hi[0] + 1))
+        nm = int(rng.integers(size_lo[1], size_hi[1] + 1))
+        fv, fr, fh = rng.uniform(0.85, 1.15, size=3)
+        out.append(hurricane(mm=mm, nm=nm, hours=hours, dx=dx, seed=seed + m, dtg=dtg, vmax=50.0 * fv,
+                             rmax=30e3 * fr, heading_scale=fh, warm=warm, **kw))
+    return out
+
+
+__all__ = ["Case", "fetch_limited", "random_field", "hurricane", "ensemble_members", "jonswap_state", "unroll", "sea_mask_from_z",
            "spectral_grid", "wavenumber", "DEFAULTS"]

@@ -167,30 +167,33 @@ void collect_timings(Model& M) {
   M.evused = 0;
 }
 
-// per-(o,i) tables in the blocked device layout [o][j/32][t][32].  A member's
-// ghost point holds the ghost values of cp0/cg0; padding points get finite
-// throw-away values (k = 1) so that idle lanes stay finite.
-std::vector<float> build_tables(const Model& M) {
+// per-(o,i) tables in the blocked device layout [o][j/32][t][32], one member
+// at a time (host memory of one member).  A member's ghost point holds the
+// ghost values of cp0/cg0; padding points get finite throw-away values (k = 1)
+// so that idle lanes stay finite.  Members start on a tile boundary, so for
+// each o a member's blocks are one contiguous range.
+int upload_tables(Model& M, const MemberHost& mh) {
   const Params& prm = M.prm;
   const int O = prm.O;
-  std::vector<float> T((size_t)O * prm.NB * T_COUNT * 32, 0.f);
-  for (const MemberHost& mh : M.mem) {
-    const HostModel& H = mh.H;
-    const std::vector<float>* src[T_COUNT] = {&H.k, &H.cp0, &H.cg0, &H.logl2overz, &H.fkovg, &H.k4, &H.k3dk,
-                                              &H.kdk, &H.cothkd, &H.sbf, &H.sdv, &H.bf1r, &H.bf2r};
-    for (int o = 1; o <= O; ++o)
-      for (int t = 0; t < T_COUNT; ++t) {
-        const bool ghost = (t == T_CP0 || t == T_CG0);
-        for (int j = 0; j < mh.padded; ++j) {
-          float v;
-          if (j < mh.N) v = (*src[t])[H.oi(o, j + 1)];
-          else if (ghost) v = (*src[t])[H.oi(o, 0)];
-          else v = (t == T_K || t == T_K4 || t == T_KDK || t == T_COTHKD) ? 1.f : 0.f;
-          T[tidx(prm, o - 1, t, mh.off + j)] = v;
-        }
+  const HostModel& H = mh.H;
+  const std::vector<float>* src[T_COUNT] = {&H.k, &H.cp0, &H.cg0, &H.logl2overz, &H.fkovg, &H.k4, &H.k3dk,
+                                            &H.kdk, &H.cothkd, &H.sbf, &H.sdv, &H.bf1r, &H.bf2r};
+  const size_t per_o = (size_t)mh.padded * T_COUNT;  // floats of one level of this member
+  std::vector<float> T(per_o);
+  for (int o = 1; o <= O; ++o) {
+    for (int t = 0; t < T_COUNT; ++t) {
+      const bool ghost = (t == T_CP0 || t == T_CG0);
+      for (int j = 0; j < mh.padded; ++j) {
+        float v;
+        if (j < mh.N) v = (*src[t])[H.oi(o, j + 1)];
+        else if (ghost) v = (*src[t])[H.oi(o, 0)];
+        else v = (t == T_K || t == T_K4 || t == T_KDK || t == T_COTHKD) ? 1.f : 0.f;
+        T[((size_t)(j >> 5) * T_COUNT + t) * 32 + (j & 31)] = v;
       }
+    }
+    CU(cudaMemcpy(M.TAB + tidx(prm, o - 1, 0, mh.off), T.data(), per_o * 4, cudaMemcpyHostToDevice));
   }
-  return T;
+  return UMWM_OK;
 }
 
 int set_forcing_constants(Model& M, MemberHost& mh) {
@@ -357,12 +360,10 @@ int init_device(Model& M) {
   CU(D.alloc(&M.ES, spec, false));
   P.E = M.E; P.ES = M.ES;
   P.EF = M.E;  // ef overwrites e bin by bin (source integration), e overwrites ef (advection)
-  CU(D.alloc(&M.TAB, (size_t)p.O * T_COUNT * ldN, false));
+  CU(D.alloc(&M.TAB, (size_t)p.O * T_COUNT * ldN, true));
   P.TAB = M.TAB;
-  {
-    std::vector<float> T = build_tables(M);
-    CU(cudaMemcpy(M.TAB, T.data(), T.size() * 4, cudaMemcpyHostToDevice));
-  }
+  for (const MemberHost& mh : M.mem)
+    if ((rc = upload_tables(M, mh))) return rc;
   // per-point arrays in the common index space
   auto upload_i = [&](const int** dst, std::vector<int>(HostModel::*field), bool aliased) -> int {
     std::vector<int> h(ldN, 0);
