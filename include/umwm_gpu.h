@@ -170,6 +170,59 @@ double umwm_gpu_get_stat(const char* name);
 /* Message of the last failure ("" if none). */
 const char* umwm_gpu_last_error(void);
 
+/* ---- learned source-term surrogate --------------------------------------
+ * No counterpart in the reference: an MLP (om*pm + 9 inputs padded to 1344
+ * -> 512 -> 512 -> 1344, GELU; bf16 operands, f32 accumulation on the tensor
+ * cores) that replaces the source-term integration of a substep
+ * (umwm_physics.F90:61-84) when the option "surrogate" is 1.  Inputs of a
+ * point: its log-spectrum rotated so the wind lies along the first
+ * direction, wind speed, the wind's offset from that direction, friction
+ * velocity, log depth, dts, currents along/across the wind, rhoa/rhow and
+ * ice fraction.  Output: the step's log-tendency, ef = (e+eps) exp(2 y) - eps.
+ * A per-point energy-budget monitor (|ln(sum ef kdk / sum e kdk)| <=
+ * "surrogate_tol", default 0.1) sends a point that fails back to the plain
+ * integration.  get_stat "surrogate_points" / "surrogate_fallback" count
+ * point-substeps since the surrogate buffers were created. */
+
+/* Create the network for om x pm spectra with seeded random weights (and
+ * fresh Adam state).  Parameters persist across initialize/finalize. */
+int umwm_gpu_surrogate_init(int om, int pm, unsigned long long seed);
+
+/* Parameters as f32 in the order W1 (512 x 1344), b1 (512), W2 (512 x 512),
+ * b2 (512), W3 (1344 x 512), b3 (1344); n must be get_stat
+ * "surrogate_nparams". */
+int umwm_gpu_surrogate_get_params(float* out, long n);
+int umwm_gpu_surrogate_set_params(const float* in, long n);
+
+/* Capture training pairs during subsequent plain runs: each substep, the
+ * inputs of points_per_substep random wet points and the log-tendency the
+ * plain integration gives them, into a device store of `capacity` pairs
+ * (a new capacity empties the store; capacity 0 stops capturing). */
+int umwm_gpu_surrogate_capture(long capacity, int points_per_substep);
+
+/* Train on the captured pairs: `steps` Adam steps (learning rate lr) on
+ * mini-batches of `batch` pairs drawn with the seed; losses[steps] (may be
+ * NULL) receives the mean-squared error of each step.  batch % 128 == 0. */
+int umwm_gpu_surrogate_train(int steps, int batch, double lr, unsigned long long seed, float* losses);
+
+/* Network output (n x 1344 f32) for input rows X (n x 1344 f32; rounded
+ * to bf16 like every input). */
+int umwm_gpu_surrogate_forward(const float* X, int n, float* Y);
+
+/* Mean-squared-error loss and its gradient (get_stat "surrogate_nparams"
+ * floats, parameter order) for one batch X, T (n x 1344 f32, n % 64 == 0),
+ * without updating the parameters. */
+int umwm_gpu_surrogate_grad(const float* X, const float* T, int n, float* loss, float* grad);
+
+/* Input rows of the surrogate (im x 1344 f32) for the selected member's
+ * wet points in the current state, with the dts of the last substep. */
+int umwm_gpu_surrogate_features(float* X, long n);
+
+/* C = A B^T on the tensor cores: A (M x K) and B (N x K) bf16 bit
+ * patterns, C (M x N) f32.  K % 64 == 0, N % 32 == 0.  The GEMM the
+ * surrogate's layers use. */
+int umwm_gpu_gemm_bf16(const unsigned short* A, const unsigned short* B, float* C, int M, int N, int K);
+
 #ifdef __cplusplus
 }
 #endif

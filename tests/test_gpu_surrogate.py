@@ -1,0 +1,150 @@
+"""Learned source-term surrogate on the GPU against its CPU oracle
+(oracle/mlp_oracle.py), through the C ABI.
+
+  * the tcgen05 GEMM against an f64 product of the same bf16 operands;
+  * the surrogate's input rows against the oracle's features of the state
+    read back from the model;
+  * the forward pass and the loss gradient against the oracle, which rounds
+    to bf16 at the same points as the GPU (tolerances below);
+  * training on pairs captured from the plain model lowers the loss, and a
+    run with the trained network is closer to the plain model than a run
+    with the untrained network (the method without training).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mo():
+    from oracle import mlp_oracle
+
+    return mlp_oracle
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (300, 256, 192), (1000, 1344, 512), (4096, 512, 1344)])
+def test_gemm_bf16(lib_built, mo, M, N, K):
+    U = lib_built
+    rng = np.random.default_rng(M + N + K)
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((N, K)).astype(np.float32)
+    C = U.gemm_bf16(mo.bf16_bits(A), mo.bf16_bits(B))
+    ref = mo.bf16(A).astype(np.float64) @ mo.bf16(B).astype(np.float64).T
+    # f32 accumulation of K exact bf16 products
+    assert np.abs(C - ref).max() <= 1e-5 * np.abs(ref).max() * np.sqrt(K / 64.0) + 1e-6
+
+
+def _batch(mo, n, seed):
+    rng = np.random.default_rng(seed)
+    X = np.zeros((n, mo.FPAD), np.float32)
+    X[:, :1332 + mo.NEXTRA] = rng.standard_normal((n, 1332 + mo.NEXTRA)).astype(np.float32)
+    T = np.zeros((n, mo.FPAD), np.float32)
+    T[:, :1332] = 0.3 * rng.standard_normal((n, 1332)).astype(np.float32)
+    return X, T
+
+
+def test_forward_matches_oracle(lib_built, mo):
+    U = lib_built
+    U.surrogate_init(37, 36, seed=5)
+    w = U.surrogate_get_params()
+    # a larger output layer than the initial one, so the outputs are O(1)
+    w[mo.OFF_W3:mo.OFF_B3] *= 10.0
+    U.surrogate_set_params(w)
+    X, _ = _batch(mo, 384, 1)
+    Y = U.surrogate_forward(X)
+    Yo, _ = mo.forward(w, X)
+    # bf16 hidden activations: a last-place difference in an f32 sum can flip
+    # one bf16 rounding, so compare in norm (and bound the worst element)
+    rel = np.linalg.norm(Y - Yo) / np.linalg.norm(Yo)
+    assert rel < 2e-3, rel
+    assert np.abs(Y - Yo).max() < 2e-2 * np.abs(Yo).max()
+
+
+def test_gradient_matches_oracle(lib_built, mo):
+    U = lib_built
+    U.surrogate_init(37, 36, seed=7)
+    w = U.surrogate_get_params()
+    w[mo.OFF_W3:mo.OFF_B3] *= 10.0
+    U.surrogate_set_params(w)
+    X, T = _batch(mo, 256, 2)
+    loss, g = U.surrogate_grad(X, T)
+    lo, go = mo.loss_and_grad(w, X, T, 1332)
+    assert abs(loss - lo) <= 1e-3 * lo
+    for name, a, b in (("W1", mo.OFF_W1, mo.OFF_B1), ("b1", mo.OFF_B1, mo.OFF_W2), ("W2", mo.OFF_W2, mo.OFF_B2),
+                       ("b2", mo.OFF_B2, mo.OFF_W3), ("W3", mo.OFF_W3, mo.OFF_B3), ("b3", mo.OFF_B3, mo.NPARAM)):
+        rel = np.linalg.norm(g[a:b] - go[a:b]) / np.linalg.norm(go[a:b])
+        assert rel < 2e-2, (name, rel)
+
+
+def test_features_match_oracle(lib_built, mo):
+    from umwm_gb300 import configs
+
+    U = lib_built
+    case = configs.hurricane(mm=40, nm=36, hours=1, dx=4000.0, dtg=600, seed=3)
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=case.nml)
+    U.set_option("max_substeps", 3)
+    U.umwm_run(case.start, case.stop)
+    Xg = U.surrogate_features()
+    F, ust = U.get_state()
+    im = F.shape[0]
+    g = {k: U.get_field(k)[:im] for k in ("wdir", "wspd", "uc", "vc", "rhorat", "fice")}
+    Xo, _ = mo.features(F, g["wdir"].astype(np.float64), g["wspd"], ust, U.get_field("d")[:im], U.get_field("dts"),
+                        g["uc"], g["vc"], g["rhorat"], g["fice"], U.get_field("th").astype(np.float64),
+                        float(U.get_field("dth")))
+    U.umwm_finalize()
+    # the GPU rounds its f32 feature to bf16: one bf16 step apart at most
+    tol = np.abs(Xo) * 2.0 ** -7 + 1e-6
+    bad = np.abs(Xg - Xo) > tol
+    assert bad.mean() < 1e-4, (bad.sum(), np.argwhere(bad)[:5])
+
+
+def test_training_and_surrogate_run(lib_built):
+    from umwm_gb300 import configs
+
+    U = lib_built
+    case = configs.random_field(mm=64, nm=56, hours=3, dx=2000.0, seed=4)
+    U.surrogate_init(37, 36, seed=11)
+    w0 = U.surrogate_get_params()
+    U.surrogate_capture(200000, 1024)
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=case.nml)
+    U.umwm_run(case.start, case.stop)
+    U.umwm_finalize()
+    U.surrogate_capture(0, 0)
+    pairs = int(U.stat("surrogate_pairs"))
+    assert pairs > 50000
+    losses = U.surrogate_train(400, batch=1024, lr=1e-3, seed=1)
+    assert np.isfinite(losses).all()
+    assert losses[-20:].mean() < 0.5 * losses[:20].mean(), (losses[:5], losses[-5:])
+    w1 = U.surrogate_get_params()
+
+    def run(surrogate, params=None):
+        if params is not None:
+            U.surrogate_set_params(params)
+        U.clear_inputs()
+        case.stage(U)
+        U.umwm_initialize(nml_text=case.nml)
+        U.set_option("surrogate", 1 if surrogate else 0)
+        stop = configs._time_str(case.start, 3600)
+        U.umwm_run(case.start, stop)
+        ht = U.get_field("ht")
+        U.set_option("surrogate", 0)
+        U.umwm_finalize()
+        return ht
+
+    ht_plain = run(False)
+    p0 = U.stat("surrogate_points")
+    f0 = U.stat("surrogate_fallback")
+    ht_trained = run(True, w1)
+    pts = U.stat("surrogate_points") - p0
+    fb = U.stat("surrogate_fallback") - f0
+    ht_untrained = run(True, w0)
+    assert np.isfinite(ht_trained).all()
+    e_tr = np.abs(ht_trained - ht_plain).mean() / ht_plain.mean()
+    e_un = np.abs(ht_untrained - ht_plain).mean() / ht_plain.mean()
+    assert pts > 0 and 0 <= fb <= pts
+    assert e_tr < e_un, (e_tr, e_un, fb / pts)

@@ -125,6 +125,10 @@ struct Ptrs {
   float *ht, *mwp, *mwd, *mss, *mwl, *dwd, *dwl, *dwp, *dcp0, *dcp, *dcg0, *dcg, *momx, *momy, *cgmxx, *cgmxy,
       *cgmyy;
   Global* glob;
+  // surrogate fallback (null otherwise): the source integration runs only
+  // tiles with fb_tile[t] != 0 and writes only points with fb_pt[j] != 0
+  const int* fb_tile;
+  const unsigned char* fb_pt;
 };
 
 // element offsets in the blocked layouts

@@ -103,9 +103,10 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
   Ctl* ctl = Mb.ctl;
   // members that have finished the current dtg sit the substep out
   if (INTEG ? !ctl->running : ctl->done) return;
+  if (INTEG && P.fb_tile && !P.fb_tile[blockIdx.x]) return;  // surrogate fallback: flagged tiles only
   const int N = Mb.ghost;  // this member's ghost point (its wet points end here)
   const int j = blockIdx.x * PTS + w * 16 + j16;
-  const bool valid = j < N;
+  const bool valid = j < N && (!INTEG || !P.fb_pt || P.fb_pt[j]);
   const int jj = valid ? j : N;  // the ghost keeps loads in bounds
   const int ja = apt(Mb, jj);
   const float sg = half ? -1.f : 1.f;

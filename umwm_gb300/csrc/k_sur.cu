@@ -1,0 +1,343 @@
+// Kernels of the source-term surrogate around the tensor-core GEMMs: input
+// features from the spectrum, targets of captured training pairs, the
+// apply step with its energy-budget monitor, and the training helpers
+// (row gather, transpose, loss, column sums, Adam, bf16 conversion).
+#include <cfloat>
+#include <cstdint>
+
+#include "dev_common.cuh"
+#include "surrogate.hpp"
+
+namespace umwm {
+namespace sur {
+
+namespace {
+
+constexpr int PITCHW = FPAD / 2 + 1;  // 32-bit words per staged row (odd: conflict-free columns)
+constexpr int TILE_SMEM = 32 * PITCHW * 4;
+
+struct PointInfo {
+  int j, ok, s;
+  float psi;
+};
+
+// Validity, rotation and wind direction of global point j.
+__device__ __forceinline__ PointInfo point_info(const Params& prm, const Ptrs& P, int j) {
+  PointInfo q{j, 0, 0, 0.f};
+  if (j < 0 || j >= prm.Ntot) return q;
+  const Member& M = prm.mem[prm.tile_mem[j / TILE]];
+  if (j >= M.off + M.N || !M.ctl->running) return q;
+  q.ok = 1;
+  q.psi = P.wdir[apt(M, j)];
+  int s = static_cast<int>(floorf((q.psi - prm.th[0]) / prm.dth + 0.5f)) % prm.P;
+  if (s < 0) s += prm.P;
+  q.s = s;
+  return q;
+}
+
+__device__ __forceinline__ float feature(float e) { return (logf(e + EPS) - LN_C0) * (1.f / LN_C1); }
+
+__device__ __forceinline__ __nv_bfloat16* row_h(uint32_t* tile, int r) {
+  return reinterpret_cast<__nv_bfloat16*>(tile + r * PITCHW);
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(256) k_features(const Params prm, const Ptrs P, const int* pts, int n,
+                                                  __nv_bfloat16* X, float* ecopy, int* shift) {
+  extern __shared__ uint32_t tile[];
+  __shared__ int s_j[32], s_ok[32], s_s[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int r0 = blockIdx.x * 32;
+  const int NP = prm.P, F0 = prm.O * prm.P;
+  if (warp == 0) {
+    const int r = r0 + lane;
+    PointInfo q{-1, 0, 0, 0.f};
+    if (r < n) q = point_info(prm, P, pts ? pts[r] : r);
+    s_j[lane] = q.j;
+    s_ok[lane] = q.ok;
+    s_s[lane] = q.s;
+    if (shift && r < n) shift[r] = q.ok ? q.s : -1;
+    float ex[NEXTRA] = {0.f};
+    if (q.ok) {
+      const int j = q.j;
+      const Member& M = prm.mem[prm.tile_mem[j / TILE]];
+      const int ja = apt(M, j);
+      float d = q.psi - prm.th[q.s];
+      d = d - 6.28318531f * floorf(d / 6.28318531f + 0.5f);
+      const float cs = cosf(q.psi), sn = sinf(q.psi);
+      ex[0] = P.wspd[ja] * (1.f / 25.f);
+      ex[1] = d / prm.dth;
+      ex[2] = P.ustar[j];
+      ex[3] = logf(P.d[j]) * 0.125f;
+      ex[4] = M.ctl->dts * (1.f / 60.f);
+      ex[5] = P.uc[ja] * cs + P.vc[ja] * sn;
+      ex[6] = -P.uc[ja] * sn + P.vc[ja] * cs;
+      ex[7] = P.rhorat[ja] * 800.f;
+      ex[8] = P.fice[ja];
+    }
+    __nv_bfloat16* h = row_h(tile, lane);
+    for (int c = F0; c < FPAD; ++c) h[c] = __float2bfloat16_rn(c - F0 < NEXTRA ? ex[c - F0] : 0.f);
+  }
+  __syncthreads();
+  const int j = s_j[lane], ok = s_ok[lane], s = s_s[lane];
+  __nv_bfloat16* h = row_h(tile, lane);
+  for (int b = warp; b < F0; b += 8) {
+    const int o = b / NP, p = b - o * NP;
+    int pr = p - s;
+    if (pr < 0) pr += NP;
+    const float e = ok ? P.E[sidx(prm, o, p, j)] : 0.f;
+    h[o * NP + pr] = __float2bfloat16_rn(ok ? feature(e) : 0.f);
+    if (ecopy && r0 + lane < n) ecopy[(size_t)(r0 + lane) * F0 + o * NP + pr] = e;
+  }
+  __syncthreads();
+  uint32_t* X32 = reinterpret_cast<uint32_t*>(X);
+  for (int rr = warp; rr < 32; rr += 8) {
+    if (r0 + rr >= n) break;
+    for (int k = lane; k < FPAD / 2; k += 32) X32[(size_t)(r0 + rr) * (FPAD / 2) + k] = tile[rr * PITCHW + k];
+  }
+}
+
+__global__ void k_targets(const Params prm, const Ptrs P, const int* pts, int n, const float* ecopy,
+                          const int* shift, __nv_bfloat16* T) {
+  const int NP = prm.P, F0 = prm.O * prm.P;
+  const size_t total = (size_t)n * FPAD;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const int r = static_cast<int>(idx / FPAD), c = static_cast<int>(idx % FPAD);
+    float t = 0.f;
+    const int s = shift[r];
+    if (c < F0 && s >= 0) {
+      const int o = c / NP, pr = c - o * NP;
+      int p = pr + s;
+      if (p >= NP) p -= NP;
+      const float ef = P.EF[sidx(prm, o, p, pts[r])];
+      t = (logf(ef + EPS) - logf(ecopy[(size_t)r * F0 + c] + EPS)) * (1.f / TS);
+    }
+    T[idx] = __float2bfloat16_rn(t);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, const __nv_bfloat16* Y, float tol,
+                                               unsigned char* fb_pt, int* fb_tile, unsigned long long* counts) {
+  extern __shared__ uint32_t tile[];
+  __shared__ float red0[8][32], red1[8][32];
+  __shared__ int s_ok[32], s_s[32], s_pass[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int jb = blockIdx.x, j = jb * 32 + lane;
+  const int NP = prm.P, F0 = prm.O * prm.P;
+  if (warp == 0) {
+    const PointInfo q = point_info(prm, P, j);
+    s_ok[lane] = q.ok;
+    s_s[lane] = q.s;
+  }
+  const uint32_t* Y32 = reinterpret_cast<const uint32_t*>(Y);
+  for (int rr = warp; rr < 32; rr += 8)
+    for (int k = lane; k < FPAD / 2; k += 32) tile[rr * PITCHW + k] = Y32[(size_t)(jb * 32 + rr) * (FPAD / 2) + k];
+  __syncthreads();
+  const int ok = s_ok[lane], s = s_s[lane];
+  const __nv_bfloat16* h = row_h(tile, lane);
+  float m0 = 0.f, m1 = 0.f;
+  if (ok) {
+    for (int b = warp; b < F0; b += 8) {
+      const int o = b / NP, p = b - o * NP;
+      int pr = p - s;
+      if (pr < 0) pr += NP;
+      const float e = P.E[sidx(prm, o, p, j)];
+      const float ef = fmaxf((e + EPS) * expf(TS * __bfloat162float(h[o * NP + pr])) - EPS, 0.f);
+      const float kdk = P.TAB[tidx(prm, o, T_KDK, j)];
+      m0 += e * kdk;
+      m1 += ef * kdk;
+    }
+  }
+  red0[warp][lane] = m0;
+  red1[warp][lane] = m1;
+  __syncthreads();
+  if (warp == 0) {
+    float a = 0.f, b = 0.f;
+    for (int w = 0; w < 8; ++w) {
+      a += red0[w][lane];
+      b += red1[w][lane];
+    }
+    const bool pass = ok && isfinite(b) && fabsf(logf((b + 1e-30f) / (a + 1e-30f))) <= tol;
+    s_pass[lane] = pass ? 1 : 0;
+    if (j < prm.Ntot) fb_pt[j] = (ok && !pass) ? 1 : 0;
+    const unsigned fails = __ballot_sync(0xffffffffu, ok && !pass);
+    const unsigned passes = __ballot_sync(0xffffffffu, pass);
+    if (lane == 0) {
+      if (fails) fb_tile[(jb * 32) / TILE] = 1;
+      if (passes) atomicAdd(&counts[0], (unsigned long long)__popc(passes));
+      if (fails) atomicAdd(&counts[1], (unsigned long long)__popc(fails));
+    }
+  }
+  __syncthreads();
+  if (!s_pass[lane]) return;
+  for (int b = warp; b < F0; b += 8) {
+    const int o = b / NP, p = b - o * NP;
+    int pr = p - s;
+    if (pr < 0) pr += NP;
+    const size_t k = sidx(prm, o, p, j);
+    const float e = P.E[k];
+    const float ef = fmaxf((e + EPS) * expf(TS * __bfloat162float(h[o * NP + pr])) - EPS, 0.f);
+    P.ES[k] = 0.5f * (e + ef);
+    P.EF[k] = ef;
+  }
+}
+
+// ---- training helpers ---------------------------------------------------------
+
+__global__ void k_gather_rows(const uint4* src, const int* idx, int n, int w16, uint4* dst) {
+  const size_t total = (size_t)n * w16;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = i / w16, c = i % w16;
+    dst[i] = src[(size_t)idx[r] * w16 + c];
+  }
+}
+
+__global__ void k_transpose(const __nv_bfloat16* src, int rows, int cols, __nv_bfloat16* dst) {
+  __shared__ __nv_bfloat16 t[32][34];
+  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int r = r0 + k, c = c0 + threadIdx.x;
+    if (r < rows && c < cols) t[k][threadIdx.x] = src[(size_t)r * cols + c];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += blockDim.y) {
+    const int c = c0 + k, r = r0 + threadIdx.x;
+    if (r < rows && c < cols) dst[(size_t)c * rows + r] = t[threadIdx.x][k];
+  }
+}
+
+__global__ void k_loss(const float* Y, const __nv_bfloat16* T, int n, int f0, __nv_bfloat16* dY, float* loss) {
+  __shared__ float red[256];
+  const size_t total = (size_t)n * FPAD;
+  const float inv = 1.f / ((float)n * f0);
+  float acc = 0.f;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = static_cast<int>(i % FPAD);
+    const float d = c < f0 ? Y[i] - __bfloat162float(T[i]) : 0.f;
+    acc += d * d;
+    dY[i] = __float2bfloat16_rn(2.f * d * inv);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(loss, red[0] * inv);
+}
+
+__global__ void k_colsum(const __nv_bfloat16* A, int rows, int cols, float* out) {
+  const int c = blockIdx.x * 32 + threadIdx.x;
+  const int r0 = blockIdx.y * 256;
+  if (c >= cols) return;
+  float acc = 0.f;
+  for (int r = r0 + threadIdx.y; r < min(rows, r0 + 256); r += blockDim.y) acc += __bfloat162float(A[(size_t)r * cols + c]);
+  atomicAdd(&out[c], acc);
+}
+
+__global__ void k_adam(float* w, const float* g, float* m, float* v, long n, float lr, float b1, float b2, float eps,
+                       float c1, float c2) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    w[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+__global__ void k_to_bf16(const float* w, int rows, int cols, __nv_bfloat16* out, __nv_bfloat16* out_t) {
+  const long total = (long)rows * cols;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const __nv_bfloat16 b = __float2bfloat16_rn(w[i]);
+    out[i] = b;
+    if (out_t) {
+      const long r = i / cols, c = i % cols;
+      out_t[c * rows + r] = b;
+    }
+  }
+}
+
+// ---- launchers ----------------------------------------------------------------
+
+static int grid_for(size_t n, int block) {
+  size_t g = (n + block - 1) / block;
+  if (g > 152u * 32) g = 152u * 32;
+  return static_cast<int>(g < 1 ? 1 : g);
+}
+
+cudaError_t launch_features(const Params& prm, const Ptrs& P, const int* pts, int n, __nv_bfloat16* X,
+                            float* ecopy, int* shift, cudaStream_t st) {
+  static cudaError_t attr = cudaFuncSetAttribute(k_features, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_SMEM);
+  if (attr != cudaSuccess) return attr;
+  if (prm.O * prm.P + NEXTRA > FPAD) return cudaErrorInvalidValue;
+  if (n <= 0) return cudaSuccess;
+  k_features<<<(n + 31) / 32, 256, TILE_SMEM, st>>>(prm, P, pts, n, X, ecopy, shift);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_targets(const Params& prm, const Ptrs& P, const int* pts, int n, const float* ecopy,
+                           const int* shift, __nv_bfloat16* T, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_targets<<<grid_for((size_t)n * FPAD, 256), 256, 0, st>>>(prm, P, pts, n, ecopy, shift, T);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_apply(const Params& prm, const Ptrs& P, const __nv_bfloat16* Y, float tol, unsigned char* fb_pt,
+                         int* fb_tile, unsigned long long* counts, cudaStream_t st) {
+  static cudaError_t attr = cudaFuncSetAttribute(k_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_SMEM);
+  if (attr != cudaSuccess) return attr;
+  k_apply<<<prm.NB, 256, TILE_SMEM, st>>>(prm, P, Y, tol, fb_pt, fb_tile, counts);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_rows(const __nv_bfloat16* src, const int* idx, int n, int width, __nv_bfloat16* dst,
+                               cudaStream_t st) {
+  if (width % 8) return cudaErrorInvalidValue;
+  const int w16 = width / 8;
+  k_gather_rows<<<grid_for((size_t)n * w16, 256), 256, 0, st>>>(reinterpret_cast<const uint4*>(src), idx, n, w16,
+                                                                reinterpret_cast<uint4*>(dst));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transpose(const __nv_bfloat16* src, int rows, int cols, __nv_bfloat16* dst, cudaStream_t st) {
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+  k_transpose<<<grid, block, 0, st>>>(src, rows, cols, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_loss(const float* Y, const __nv_bfloat16* T, int n, int f0, __nv_bfloat16* dY, float* loss,
+                        cudaStream_t st) {
+  k_loss<<<grid_for((size_t)n * FPAD, 256), 256, 0, st>>>(Y, T, n, f0, dY, loss);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_colsum(const __nv_bfloat16* A, int rows, int cols, float* out, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(out, 0, (size_t)cols * sizeof(float), st);
+  if (e != cudaSuccess) return e;
+  dim3 grid((cols + 31) / 32, (rows + 255) / 256), block(32, 8);
+  k_colsum<<<grid, block, 0, st>>>(A, rows, cols, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adam(float* w, const float* g, float* m, float* v, long n, float lr, float b1, float b2, float eps,
+                        float c1, float c2, cudaStream_t st) {
+  k_adam<<<grid_for((size_t)n, 256), 256, 0, st>>>(w, g, m, v, n, lr, b1, b2, eps, c1, c2);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_bf16(const float* w, int rows, int cols, __nv_bfloat16* out, __nv_bfloat16* out_t,
+                           cudaStream_t st) {
+  k_to_bf16<<<grid_for((size_t)rows * cols, 256), 256, 0, st>>>(w, rows, cols, out, out_t);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_f32_to_bf16(const float* a, long n, __nv_bfloat16* out, cudaStream_t st) {
+  k_to_bf16<<<grid_for((size_t)n, 256), 256, 0, st>>>(a, 1, (int)n, out, nullptr);
+  return cudaGetLastError();
+}
+
+}  // namespace sur
+}  // namespace umwm

@@ -22,6 +22,7 @@
 #include "../../include/umwm_gpu.h"
 #include "host_model.hpp"
 #include "kernels.hpp"
+#include "surrogate.hpp"
 
 namespace umwm {
 namespace {
@@ -105,6 +106,7 @@ struct Model {
   double last_gpu_ms = 0, last_bins = 0;
   long long launches = 0;
   int sel = 0;      // member the getters and setters act on
+  std::vector<std::pair<int, int>> wet_ranges;  // (off, N) of each member
   int max_nm = 0;   // largest all-point range of a member
   bool ktime = false;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> kev;  // pending (kernel, events)
@@ -299,9 +301,11 @@ int setup_params(Model& M) {
   // layout: each member's wet points, its ghost, padding to a tile
   int off = 0, nmoff = 0;
   M.max_nm = 0;
+  M.wet_ranges.clear();
   for (MemberHost& mh : M.mem) {
     mh.N = mh.H.im;
     mh.off = off;
+    M.wet_ranges.push_back({off, mh.N});
     mh.ghost = off + mh.N;
     mh.padded = (mh.N + 1 + TILE - 1) / TILE * TILE;
     off += mh.padded;
@@ -567,7 +571,18 @@ int enqueue_substep(Model& M, int compute_rot, int first, bool diag) {
   if (prm.ice_possible) CU(timed(M, K_SICE, [&] { return launch_sice(prm, P, M.st); }));
   CU(timed(M, K_PHYS, [&] { return launch_source_phys(prm, P, compute_rot, M.st); }));
   CU(timed(M, K_DTS, [&] { return launch_dts(prm, P, compute_rot, first, M.st); }));
-  CU(timed(M, K_INTEG, [&] { return launch_source_integ(prm, P, M.st); }));
+  int rc;
+  if (sur::active()) {
+    // learned source step; points outside its energy budget fall back to
+    // the plain integration (flagged tiles and points only)
+    Ptrs fbP;
+    if ((rc = sur::step(prm, P, fbP, M.st))) return rc;
+    CU(timed(M, K_INTEG, [&] { return launch_source_integ(prm, fbP, M.st); }));
+  } else {
+    if (sur::capturing() && (rc = sur::capture_before(prm, P, M.wet_ranges, M.st))) return rc;
+    CU(timed(M, K_INTEG, [&] { return launch_source_integ(prm, P, M.st); }));
+    if (sur::capturing() && (rc = sur::capture_after(prm, P, M.st))) return rc;
+  }
   CU(timed(M, K_ADVECT, [&] { return launch_advect(prm, P, M.st); }));
   if (diag) CU(timed(M, K_DIAG, [&] { return launch_diag(prm, P, M.st); }));
   CU(timed(M, K_SCREEN, [&] { return launch_screen(prm, P, M.st); }));
@@ -689,7 +704,7 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     for (long long inner = 0;;) {
       if (inner > 10000000LL) return fail(UMWM_ERR_TIMEOUT, "umwm_run: more than 1e7 substeps in one dtg (dts stuck at 0?)");
       if (M.max_substeps >= 0 && M.substeps >= M.max_substeps) return finish_run(M);
-      if (M.use_graph && !M.first && !M.ktime) {
+      if (M.use_graph && !M.first && !M.ktime && !sur::active() && !sur::capturing()) {
         if ((rc = build_graph(M))) return rc;
         long long budget = GRAPH_CHUNK;
         if (M.max_substeps >= 0) budget = std::min(budget, M.max_substeps - M.substeps);
@@ -841,6 +856,9 @@ __global__ void k_to_ref_chunk(const Params prm, const float* __restrict__ E, fl
 }
 
 }  // namespace
+
+int set_error(int code, const std::string& msg) { return fail(code, msg); }
+
 }  // namespace umwm
 
 using namespace umwm;
@@ -938,6 +956,7 @@ int umwm_gpu_run(const char* start, const char* stop) {
 
 int umwm_gpu_finalize(void) {
   g_model.reset();
+  sur::release_model_buffers();
   return UMWM_OK;
 }
 
@@ -974,6 +993,37 @@ int umwm_gpu_get_state(float* F, float* ust) {
     CU(e);
   }
   if (ust) CU(cudaMemcpy(ust, M->P.ustar + mh.off, (size_t)mh.N * 4, cudaMemcpyDeviceToHost));
+  return UMWM_OK;
+}
+
+// Surrogate input rows of the selected member's wet points for the current
+// state (the dts of the last substep), as f32 (n x 1344).
+int umwm_gpu_surrogate_features(float* X, long n) {
+  Model* M = need_model(true);
+  if (!M) return UMWM_ERR_STATE;
+  const Params& p = M->prm;
+  const MemberHost& mh = M->mem[M->sel];
+  if (!X || n != (long)mh.N * sur::FPAD) return fail(UMWM_ERR_ARG, "surrogate_features: n must be im * 1344");
+  if (p.O * p.P + sur::NEXTRA > sur::FPAD) return fail(UMWM_ERR_UNSUPPORTED, "surrogate: om*pm + 9 > 1344");
+  __nv_bfloat16* d = nullptr;
+  const size_t rows = (size_t)mh.padded;
+  CU(cudaMalloc(&d, rows * sur::FPAD * 2));
+  std::vector<int> pts(rows);
+  for (size_t r = 0; r < rows; ++r) pts[r] = mh.off + (int)r;
+  int* dp = nullptr;
+  cudaError_t e = cudaMalloc(&dp, rows * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(dp, pts.data(), rows * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = sur::launch_features(p, M->P, dp, (int)rows, d, nullptr, nullptr, M->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(M->st);
+  std::vector<uint16_t> h((size_t)mh.N * sur::FPAD);
+  if (e == cudaSuccess) e = cudaMemcpy(h.data(), d, h.size() * 2, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  cudaFree(dp);
+  CU(e);
+  for (size_t i = 0; i < h.size(); ++i) {
+    const uint32_t u = (uint32_t)h[i] << 16;
+    std::memcpy(&X[i], &u, 4);
+  }
   return UMWM_OK;
 }
 
@@ -1188,6 +1238,7 @@ int umwm_gpu_set_option(const char* name, double value) {
   if (!name) return fail(UMWM_ERR_ARG, "set_option: null name");
   std::string s(name);
   if (s == "device") { g_device = (int)value; return UMWM_OK; }
+  if (s.compare(0, 9, "surrogate") == 0) return sur::set_option(s, value);
   Model* M = g_model.get();
   if (!M) return fail(UMWM_ERR_STATE, "set_option: initialize first");
   if (s == "kernel_timing") {
@@ -1203,6 +1254,7 @@ int umwm_gpu_set_option(const char* name, double value) {
 }
 
 double umwm_gpu_get_stat(const char* name) {
+  if (name && std::strncmp(name, "surrogate", 9) == 0) return sur::get_stat(name);
   Model* M = g_model.get();
   if (!M || !name) return -1.0;
   std::string s(name);

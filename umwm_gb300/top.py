@@ -211,3 +211,75 @@ def get_screen():
         check(lib().umwm_gpu_get_screen(out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), out.size,
                                         ctypes.byref(rows)))
     return out.reshape(-1, 8)
+
+
+# ---- learned source-term surrogate -------------------------------------------
+
+SURROGATE_WIDTH = 1344
+
+
+def surrogate_init(om=37, pm=36, seed=0):
+    check(lib().umwm_gpu_surrogate_init(int(om), int(pm), int(seed)))
+
+
+def surrogate_nparams():
+    return int(stat("surrogate_nparams"))
+
+
+def surrogate_get_params():
+    out = np.zeros(surrogate_nparams(), dtype=np.float32)
+    check(lib().umwm_gpu_surrogate_get_params(out.ctypes.data_as(_fp), out.size))
+    return out
+
+
+def surrogate_set_params(w):
+    a = _f32(w).ravel()
+    check(lib().umwm_gpu_surrogate_set_params(a.ctypes.data_as(_fp), a.size))
+
+
+def surrogate_capture(capacity, points_per_substep):
+    check(lib().umwm_gpu_surrogate_capture(int(capacity), int(points_per_substep)))
+
+
+def surrogate_train(steps, batch=4096, lr=1e-3, seed=0):
+    """Adam steps on the captured pairs; returns the loss of each step."""
+    losses = np.zeros(int(steps), dtype=np.float32)
+    check(lib().umwm_gpu_surrogate_train(int(steps), int(batch), float(lr), int(seed), losses.ctypes.data_as(_fp)))
+    return losses
+
+
+def surrogate_forward(X):
+    X = _f32(X)
+    n = X.shape[0]
+    Y = np.zeros((n, SURROGATE_WIDTH), dtype=np.float32)
+    check(lib().umwm_gpu_surrogate_forward(X.ctypes.data_as(_fp), n, Y.ctypes.data_as(_fp)))
+    return Y
+
+
+def surrogate_grad(X, T):
+    X, T = _f32(X), _f32(T)
+    loss = np.zeros(1, dtype=np.float32)
+    g = np.zeros(surrogate_nparams(), dtype=np.float32)
+    check(lib().umwm_gpu_surrogate_grad(X.ctypes.data_as(_fp), T.ctypes.data_as(_fp), X.shape[0],
+                                        loss.ctypes.data_as(_fp), g.ctypes.data_as(_fp)))
+    return float(loss[0]), g
+
+
+def surrogate_features():
+    """Surrogate input rows (im, 1344) of the selected member's current state."""
+    n = dims()["im"]
+    X = np.zeros((n, SURROGATE_WIDTH), dtype=np.float32)
+    check(lib().umwm_gpu_surrogate_features(X.ctypes.data_as(_fp), X.size))
+    return X
+
+
+def gemm_bf16(A_bits, B_bits):
+    """C = A B^T on the tensor cores; A (M, K), B (N, K) as uint16 bf16 bit patterns."""
+    A = np.ascontiguousarray(A_bits, dtype=np.uint16)
+    B = np.ascontiguousarray(B_bits, dtype=np.uint16)
+    M, K = A.shape
+    N = B.shape[0]
+    C = np.zeros((M, N), dtype=np.float32)
+    up = ctypes.POINTER(ctypes.c_uint16)
+    check(lib().umwm_gpu_gemm_bf16(A.ctypes.data_as(up), B.ctypes.data_as(up), C.ctypes.data_as(_fp), M, N, K))
+    return C
