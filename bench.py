@@ -311,6 +311,120 @@ def run_ensemble(args):
     return 0
 
 
+def peak_bf16():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops"]), float(d.get("bf16_tflops_sustained", d["bf16_tflops"])), "measured"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, 1700.0, "fallback"
+
+
+def _angle_err_deg(a, b):
+    d = np.angle(np.exp(1j * (np.asarray(a, np.float64) - np.asarray(b, np.float64))))
+    return np.degrees(np.abs(d))
+
+
+def run_surrogate(args):
+    """Learned source-term surrogate (hurricane forcing on the size x size
+    grid).  Pairs come from plain GPU runs of a random-field domain and a
+    hurricane domain with other seeds; the network trains on the GPU; then
+    the same hurricane case runs args.hours with the plain path and with the
+    surrogate (energy-budget fallback on), and the surrogate's Hs, Tp (peak
+    period, dwp) and mean direction are compared with the plain run."""
+    rank, world, local_rank = rank_info()
+    import umwm_gb300 as U
+    from umwm_gb300 import configs
+
+    U.set_option("device", local_rank)
+    U.surrogate_init(37, 36, seed=7)
+    U.surrogate_capture(args.pairs, args.pts_per_substep)
+    gen = []
+    t0 = time.perf_counter()
+    for make in (lambda: configs.random_field(mm=args.size, nm=args.size, hours=1, seed=21),
+                 lambda: configs.hurricane(mm=800, nm=800, hours=3, seed=31)):
+        case = make()
+        U.clear_inputs()
+        case.stage(U)
+        U.umwm_initialize(nml_text=case.nml)
+        U.umwm_run(case.start, case.stop)
+        gen.append({"case": case.name, "substeps": U.dims()["substeps"], "pairs_after": int(U.stat("surrogate_pairs"))})
+        U.umwm_finalize()
+        del case
+    U.surrogate_capture(0, 0)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    l1 = U.surrogate_train(args.train_steps, batch=8192, lr=1e-3, seed=1)
+    l2 = U.surrogate_train(args.train_steps // 2, batch=8192, lr=2e-4, seed=2)
+    t_train = time.perf_counter() - t0
+    losses = np.concatenate([l1, l2])
+
+    ev = configs.hurricane(mm=args.size, nm=args.size, hours=args.hours, seed=5)
+
+    def run(sur):
+        U.clear_inputs()
+        ev.stage(U)
+        U.umwm_initialize(nml_text=ev.nml)
+        U.set_option("use_graph", 0 if sur else 1)
+        U.set_option("surrogate", 1 if sur else 0)
+        U.set_option("surrogate_timing", 1 if sur else 0)
+        p0, f0 = U.stat("surrogate_points"), U.stat("surrogate_fallback")
+        U.umwm_run(ev.start, ev.stop)
+        out = {"gpu_ms": U.stat("gpu_ms"), "bins": U.stat("bin_updates"), "substeps": U.dims()["substeps"],
+               "ht": U.get_field("ht"), "dwp": U.get_field("dwp"), "mwd": U.get_field("mwd"),
+               "points": U.stat("surrogate_points") - p0, "fallback": U.stat("surrogate_fallback") - f0}
+        if sur:
+            out.update({k: U.stat("surrogate_" + k) for k in ("ms_features", "ms_gemm", "ms_apply", "timed_steps",
+                                                              "rows")})
+        U.set_option("surrogate", 0)
+        U.set_option("surrogate_timing", 0)
+        U.umwm_finalize()
+        return out
+
+    plain = run(False)
+    sur = run(True)
+    hp, hs = plain["ht"].astype(np.float64), sur["ht"].astype(np.float64)
+    wet = hp > 1e-3
+    hs_err = {"mean_abs_rel": float(np.abs(hs - hp)[wet].mean() / hp[wet].mean()),
+              "rel_l2": float(np.linalg.norm((hs - hp)[wet]) / np.linalg.norm(hp[wet])),
+              "p99_rel": float(np.percentile(np.abs(hs - hp)[wet] / hp[wet], 99)),
+              "domain_mean_rel": float(abs(hs[wet].mean() - hp[wet].mean()) / hp[wet].mean())}
+    tp_err = {"mean_abs_rel": float((np.abs(sur["dwp"] - plain["dwp"])[wet] / plain["dwp"][wet]).mean()),
+              "same_bin_frac": float((sur["dwp"] == plain["dwp"])[wet].mean())}
+    dir_err = {"mean_abs_deg": float(_angle_err_deg(sur["mwd"], plain["mwd"])[wet].mean()),
+               "hs_weighted_deg": float((_angle_err_deg(sur["mwd"], plain["mwd"]) * hp)[wet].sum() / hp[wet].sum())}
+    v_sur = sur["bins"] / (sur["gpu_ms"] / 1e3)
+    v_plain = plain["bins"] / (plain["gpu_ms"] / 1e3)
+    flops_row = 2.0 * (1344 * 512 + 512 * 512 + 512 * 1344)
+    gemm_tflops = (flops_row * sur["rows"] * sur["timed_steps"] / (sur["ms_gemm"] / 1e3) / 1e12
+                   if sur["ms_gemm"] > 0 else None)
+    pk, pk_sus, pk_kind = peak_bf16()
+    line = {"metric": METRIC, "value": v_sur, "unit": UNIT, "n_gpus": 1, "steps": sur["substeps"], "warmup": 0,
+            "ms_per_step": sur["gpu_ms"] / max(sur["substeps"], 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16 (MLP) / f32 (spectrum)", "data": "synthetic",
+            "config": {"workload": "surrogate: hurricane %dx%d dx=2km seed 5, %g h, JONSWAP Hs 0.2 m start; MLP "
+                                   "1344-512-512-1344 GELU bf16/f32-acc; energy-budget tolerance 0.1"
+                                   % (args.size, args.size, args.hours),
+                       "pairs": int(U.stat("surrogate_pairs")), "pair_sources": gen,
+                       "train_steps": int(len(losses)), "batch": 8192},
+            "plain": {"value": v_plain, "gpu_ms": plain["gpu_ms"], "substeps": plain["substeps"]},
+            "surrogate_over_plain": v_sur / v_plain,
+            "fallback_fraction": sur["fallback"] / max(sur["points"], 1),
+            "hs_error_vs_plain": hs_err, "tp_error_vs_plain": tp_err, "dir_error_vs_plain": dir_err,
+            "train": {"seconds": t_train, "loss_first": float(losses[:20].mean()), "loss_last": float(losses[-20:].mean())},
+            "generate_seconds": t_gen,
+            "surrogate_ms_per_step": {"features": sur["ms_features"] / max(sur["timed_steps"], 1),
+                                      "gemm": sur["ms_gemm"] / max(sur["timed_steps"], 1),
+                                      "apply": sur["ms_apply"] / max(sur["timed_steps"], 1)},
+            "roofline": {"bound": "tensor", "kernel": "k_gemm (3 layers)", "achieved": gemm_tflops, "peak": pk_sus,
+                         "unit": "TFLOP/s", "frac": (gemm_tflops / pk_sus) if gemm_tflops else None,
+                         "peak_kind": pk_kind + " sustained", "traffic": None}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -322,7 +436,11 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="random_field", choices=["random_field", "ensemble"])
+    ap.add_argument("--workload", default="random_field", choices=["random_field", "ensemble", "surrogate"])
+    ap.add_argument("--pairs", type=int, default=2000000)
+    ap.add_argument("--pts-per-substep", type=int, default=16384)
+    ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--hours", type=float, default=12.0)
     ap.add_argument("--members", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
@@ -331,6 +449,8 @@ def main():
         return run_reference(args)
     if args.workload == "ensemble":
         return run_ensemble(args)
+    if args.workload == "surrogate":
+        return run_surrogate(args)
 
     rank, world, local_rank = rank_info()
     dist = Dist(world, local_rank)

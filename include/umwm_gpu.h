@@ -160,7 +160,11 @@ int umwm_gpu_get_screen(double* out, long n, long* rows);
  * node: one host synchronisation per outer step instead of one per
  * substep; results are bit-identical), "kernel_timing" (CUDA-event time of
  * each kernel, read with umwm_gpu_get_stat "ms:<kernel>"; the inner loop
- * then runs host-driven), "device" (CUDA device of the next initialize). */
+ * then runs host-driven), "device" (CUDA device of the next initialize),
+ * "direction_groups" (2, default: each point's directions in two half-turn
+ * groups per warp lane pair; 4: four quarter-turn groups, fewer registers
+ * per thread; needs pm % 4 == 0 and pm/4 in {4, 6, 8, 9, 12}; results differ
+ * from 2 by summation order only). */
 int umwm_gpu_set_option(const char* name, double value);
 
 /* Run statistics: "substeps", "gpu_ms" (device time of the last run),
@@ -180,8 +184,11 @@ const char* umwm_gpu_last_error(void);
  * velocity, log depth, dts, currents along/across the wind, rhoa/rhow and
  * ice fraction.  Output: the step's log-tendency, ef = (e+eps) exp(2 y) - eps.
  * A per-point energy-budget monitor (|ln(sum ef kdk / sum e kdk)| <=
- * "surrogate_tol", default 0.1) sends a point that fails back to the plain
- * integration.  get_stat "surrogate_points" / "surrogate_fallback" count
+ * "surrogate_tol", default 0.02 per substep), and the same for the energy of
+ * every frequency level holding more than 1e-4 of the point's largest
+ * ("surrogate_tol_level", default 0.1), sends a point that fails back to the
+ * plain integration.  A bin's growth is capped by its wind input,
+ * dts max(Sin, 0) + 0.02 in ln.  get_stat "surrogate_points" / "surrogate_fallback" count
  * point-substeps since the surrogate buffers were created. */
 
 /* Create the network for om x pm spectra with seeded random weights (and
@@ -204,6 +211,11 @@ int umwm_gpu_surrogate_capture(long capacity, int points_per_substep);
  * mini-batches of `batch` pairs drawn with the seed; losses[steps] (may be
  * NULL) receives the mean-squared error of each step.  batch % 128 == 0. */
 int umwm_gpu_surrogate_train(int steps, int batch, double lr, unsigned long long seed, float* losses);
+
+/* Mean-squared-error loss of the current network over the stored pairs
+ * [first, first + count) (no training).  Option "surrogate_holdout" keeps
+ * that many trailing stored pairs out of umwm_gpu_surrogate_train. */
+int umwm_gpu_surrogate_eval(long first, long count, double* loss);
 
 /* Network output (n x 1344 f32) for input rows X (n x 1344 f32; rounded
  * to bf16 like every input). */

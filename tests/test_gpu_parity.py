@@ -188,3 +188,21 @@ def test_fetch_limited_full_run_vs_fp64(U, oracle_mod):
         assert e < tol, "%s rel err %.3g" % (name, e)
     ang = np.angle(np.exp(1j * (U.get_field("mwd") - o64.get("mwd"))))
     assert np.abs(ang).max() < 0.02
+
+
+@pytest.mark.parametrize("groups", [2, 4])
+def test_direction_groups_random_field(U, oracle_mod, groups):
+    """Both thread mappings of the spectral kernels (two half-turn or four
+    quarter-turn direction groups per point) against the oracle."""
+    from umwm_gb300 import configs
+
+    case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0)
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=case.nml)
+    U.set_option("direction_groups", groups)
+    U.set_option("max_substeps", 8)
+    U.umwm_run(case.start, case.stop)
+    o = run_oracle(oracle_mod, case, 32, max_substeps=8)
+    _compare_state(U, o, 1e-4, FIELD_TOL)
+    U.umwm_finalize()

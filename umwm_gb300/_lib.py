@@ -19,7 +19,7 @@ EXPORTS = [
     "umwm_gpu_get_stat", "umwm_gpu_last_error", "umwm_gpu_ensemble_add", "umwm_gpu_ensemble_initialize",
     "umwm_gpu_select_member", "umwm_gpu_surrogate_init", "umwm_gpu_surrogate_get_params",
     "umwm_gpu_surrogate_set_params", "umwm_gpu_surrogate_capture", "umwm_gpu_surrogate_train",
-    "umwm_gpu_surrogate_forward", "umwm_gpu_surrogate_grad", "umwm_gpu_surrogate_features", "umwm_gpu_gemm_bf16",
+    "umwm_gpu_surrogate_forward", "umwm_gpu_surrogate_grad", "umwm_gpu_surrogate_features", "umwm_gpu_surrogate_eval", "umwm_gpu_gemm_bf16",
 ]
 
 ERRORS = {0: "UMWM_OK", 1: "UMWM_ERR_NAMELIST", 2: "UMWM_ERR_INPUT", 3: "UMWM_ERR_CUDA", 4: "UMWM_ERR_NONFINITE",
@@ -78,6 +78,7 @@ def lib():
         "umwm_gpu_surrogate_forward": [fp, ctypes.c_int, fp],
         "umwm_gpu_surrogate_grad": [fp, fp, ctypes.c_int, fp, fp],
         "umwm_gpu_surrogate_features": [fp, ctypes.c_long],
+        "umwm_gpu_surrogate_eval": [ctypes.c_long, ctypes.c_long, dp],
         "umwm_gpu_gemm_bf16": [ctypes.POINTER(ctypes.c_uint16), ctypes.POINTER(ctypes.c_uint16), fp, ctypes.c_int,
                                ctypes.c_int, ctypes.c_int],
     }

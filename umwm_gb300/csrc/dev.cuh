@@ -41,7 +41,13 @@ enum TableRow {
   T_COUNT
 };
 
-constexpr int TILE = 64;  // wet points per CTA tile of the spectral kernels
+constexpr int TILE = 64;  // wet points of a tile (a member's points start on a tile boundary)
+
+// Direction groups per point of the spectral kernels: 4 quarter-turn groups
+// when pm % 4 == 0 and pm/4 is a supported group size, else 2 half-turn groups.
+__host__ __device__ constexpr bool quarter_groups(int pm) {
+  return pm % 4 == 0 && (pm / 4 == 4 || pm / 4 == 6 || pm / 4 == 8 || pm / 4 == 9 || pm / 4 == 12);
+}
 
 struct Ctl;
 struct Member;
@@ -56,6 +62,7 @@ struct Params {
       sdt_fac, z, nu_air, kappa, fprog, dth, dthg, oneovdth, dtg, fice_lth, fice_uth, eulerinv, rhow0;
   int winds, currents, air_density, water_density, seaice, restart, curvilinear, isglobal;
   int ice_possible;  // fice can exceed fice_lth somewhere
+  int groups4;       // spectral kernels use 4 quarter-turn direction groups (option "direction_groups")
   float f[MAX_OM], dom[MAX_OM];
   float th[MAX_PM], cth[MAX_PM], sth[MAX_PM], c2th[MAX_PM], s2th[MAX_PM];
   float depth[MAX_LM];

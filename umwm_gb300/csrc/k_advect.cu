@@ -1,9 +1,10 @@
 // Propagation, refraction, e = ef and stress('atm') in one pass
 // (umwm_advection.F90:18-180, umwm_top.F90:113-115, umwm_stress.F90:17-264).
 //
-// Same thread mapping as the source kernels: a warp owns 16 consecutive wet
-// points, lane = point + 16 * half, half h takes directions h*H .. h*H+H-1
-// with compile-time direction constants and a per-lane sign.
+// Same thread mapping as the source kernels: G direction groups of H = pm/G
+// directions per point, lane = point + (32/G) * q, group q is the base group
+// turned by q*2pi/G (per-lane rotation ra, rb), so direction constants are
+// those of the base group and known at compile time.
 //
 // Propagation.  cg0 > 0, so for an edge velocity cge = (cg0_i + cg0_ie) c,
 // (cge + |cge|) = 2 (cg0_i + cg0_ie) max(c, 0) and (cge - |cge|) uses min(c, 0):
@@ -12,19 +13,18 @@
 // unrolled neighbours.  The east/west neighbours sit about one wet column
 // (~nm points) away and are served from L2, which holds the window of blocks
 // the CTAs in flight work on.
-// Refraction needs E* at p-1 and p+1: inside a half they are registers, at
-// the half's edges they come from the partner lane (shuffle).  The rotation
+// Refraction needs E* at p-1 and p+1: inside a group they are registers, at
+// the group's edges they come from the neighbouring groups' lanes (shuffle).  The rotation
 // rate is recomputed from cp0 and the currents (it depends on no spectral
 // value); when the reference would reuse the rotation of an earlier substep
 // (currents = .F.) the mask o <= oc of that substep is kept in oc_rot.
 // The wind stress sums e*Sin*cos/sin(th)/cp over the new spectrum while it is
-// in registers; half 0 then finishes the drag, skin stress and ustar.
+// in registers; group 0 then finishes the drag, skin stress and ustar.
 #include "dev_common.cuh"
 #include "kernels.hpp"
 
 namespace umwm {
 
-constexpr int PTS_A = TILE;  // wet points per CTA (4 warps x 16)
 
 // bulk prefetch of a contiguous, 16-byte aligned range into L2
 __device__ __forceinline__ void bulk_prefetch(const void* p, unsigned bytes) {
@@ -54,20 +54,24 @@ __device__ __forceinline__ float sin_dir(const Params& prm, const WindIn& w, flo
   return s;
 }
 
-template <int H, bool CURV>
-__global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs P) {
+template <int G, int H, bool CURV>
+__global__ void __launch_bounds__(128, G == 4 ? 4 : 3) k_advect(const Params prm, const Ptrs P) {
+  constexpr int PW = 32 / G;   // points per warp
+  constexpr int PPC = 4 * PW;  // points per CTA (4 warps)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int j16 = lane & 15, half = lane >> 4;
+  const int jl = lane % PW, q = lane / PW;
   const int O = prm.O;
-  const Member& Mb = prm.mem[prm.tile_mem[blockIdx.x]];
+  const Member& Mb = prm.mem[prm.tile_mem[(blockIdx.x * PPC) / TILE]];
   const Ctl* ctl = Mb.ctl;
   if (!ctl->running) return;  // the member has finished the current dtg
   const int N = Mb.ghost;
-  const int j = blockIdx.x * PTS_A + w * 16 + j16;
+  const int j = blockIdx.x * PPC + w * PW + jl;
   const bool valid = j < N;
   const int jj = valid ? j : N;
   const int ja = apt(Mb, jj);
-  const float sg = half ? -1.f : 1.f;
+  // rotation of this lane's group relative to the base group
+  const float ra = G == 2 ? (q ? -1.f : 1.f) : (q == 0 ? 1.f : (q == 2 ? -1.f : 0.f));
+  const float rb = G == 2 ? 0.f : (q == 1 ? 1.f : (q == 3 ? -1.f : 0.f));
   __shared__ float cws[H][128];
   __shared__ float ccs[CURV ? H : 1][128], scs[CURV ? H : 1][128];
 
@@ -82,7 +86,8 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
   const float ustar = P.ustar[jj];
   const WindIn wi = load_wind(prm, P, jj, ja, ustar);
   const float wdir = P.wdir[ja];
-  const float ucg = sg * wi.uc, vcg = sg * wi.vc;
+  const float ucg = G == 2 ? ra * wi.uc : ra * wi.uc + rb * wi.vc;
+  const float vcg = G == 2 ? ra * wi.vc : ra * wi.vc - rb * wi.uc;
 
   // current advection, umwm_advection.F90:62-82, folded per point
   float F0 = 0.f, fedn = 0.f, fwup = 0.f, fndn = 0.f, fsup = 0.f;
@@ -102,7 +107,7 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
 
 #pragma unroll
   for (int k = 0; k < H; ++k) {
-    const float th = prm.th[half * H + k];
+    const float th = prm.th[q * H + k];
     cws[k][threadIdx.x] = cosf(wdir - th);
     if (CURV) {
       const float cv = P.curv[jj];
@@ -114,7 +119,7 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
   // blocked-layout offsets of the point and its neighbours
   const size_t lstride = (size_t)prm.NB * prm.P * 32;
   const size_t tstride = (size_t)prm.NB * T_COUNT * 32;
-  const size_t hoff = (size_t)(half * H) * 32;
+  const size_t hoff = (size_t)(q * H) * 32;
   const size_t oS = sidx(prm, 0, 0, jj) + hoff, oE = sidx(prm, 0, 0, ie) + hoff, oW = sidx(prm, 0, 0, iw) + hoff,
                oN = sidx(prm, 0, 0, in) + hoff, oSs = sidx(prm, 0, 0, is) + hoff;
   // stress_vector_integral divides by cp0 of the previous unrolled point
@@ -152,8 +157,8 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
       float es[H];
 #pragma unroll
       for (int k = 0; k < H; ++k) es[k] = __ldg(ESo + oS + k * 32);
-      const float esm = __shfl_xor_sync(pm, es[H - 1], 16);  // E* at p-1 for k = 0
-      const float esp = __shfl_xor_sync(pm, es[0], 16);      // E* at p+1 for k = H-1
+      const float esm = __shfl_sync(pm, es[H - 1], (lane - PW) & 31);  // E* at p-1 for k = 0 (group q-1)
+      const float esp = __shfl_sync(pm, es[0], (lane + PW) & 31);      // E* at p+1 for k = H-1 (group q+1)
       // ---- propagation, umwm_advection.F90:30-97
       const float cgi = __ldg(T + tS + T_CG0 * 32);
       const float DE = 2.f * (cgi + __ldg(T + tE + T_CG0 * 32)) * dye;
@@ -165,8 +170,10 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
         const float e0 = es[k];
         const float ee = __ldg(ESo + oE + k * 32), ew = __ldg(ESo + oW + k * 32);
         const float en = __ldg(ESo + oN + k * 32), esn = __ldg(ESo + oSs + k * 32);
-        const float cc = CURV ? ccs[k][threadIdx.x] : sg * prm.cth[k];
-        const float sc = CURV ? scs[k][threadIdx.x] : sg * prm.sth[k];
+        const float cc = CURV ? ccs[k][threadIdx.x]
+                              : (G == 2 ? ra * prm.cth[k] : ra * prm.cth[k] - rb * prm.sth[k]);
+        const float sc = CURV ? scs[k][threadIdx.x]
+                              : (G == 2 ? ra * prm.sth[k] : rb * prm.cth[k] + ra * prm.sth[k]);
         const float cp = fmaxf(cc, 0.f), cm = fminf(cc, 0.f), sp = fmaxf(sc, 0.f), sm = fminf(sc, 0.f);
         float flux = DE * (cp * e0 + cm * ee) - DW * (cp * ew + cm * e0) + DN * (sp * e0 + sm * en) -
                      DS * (sp * esn + sm * e0);
@@ -178,15 +185,21 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
         const float gx = 0.5f * (__ldg(T + tE + T_CP0 * 32) - __ldg(T + tW + T_CP0 * 32));
         const float gy = 0.5f * (__ldg(T + tN + T_CP0 * 32) - __ldg(T + tSs + T_CP0 * 32));
         const float hbx = 0.5f * bx, hby = 0.5f * by;
-        // rotation rate at direction k of this half (sign sg) or of the partner half (-sg)
-        auto rot = [&](int k, float s) {
-          return (gx * s * prm.sth[k] + hbx) * odx - (gy * s * prm.cth[k] + hby) * ody;
+        // rotation rate at base direction k of a group turned by (ca, cb):
+        // sin th = cb cos th0 + ca sin th0, cos th = ca cos th0 - cb sin th0
+        auto rot = [&](int k, float ca, float cb) {
+          if (G == 2) return (gx * ca * prm.sth[k] + hbx) * odx - (gy * ca * prm.cth[k] + hby) * ody;
+          return (gx * (cb * prm.cth[k] + ca * prm.sth[k]) + hbx) * odx -
+                 (gy * (ca * prm.cth[k] - cb * prm.sth[k]) + hby) * ody;
         };
-        float rprev = rot(H - 1, -sg);  // p-1 of k = 0 is the partner's last direction
-        float rcur = rot(0, sg);
+        // the previous group is this one turned back by 2pi/G, the next one turned on
+        const float pa = G == 2 ? -ra : rb, pb = G == 2 ? 0.f : -ra;
+        const float na = G == 2 ? -ra : -rb, nb = G == 2 ? 0.f : ra;
+        float rprev = rot(H - 1, pa, pb);  // p-1 of k = 0 is the previous group's last direction
+        float rcur = rot(0, ra, rb);
 #pragma unroll
         for (int k = 0; k < H; ++k) {
-          const float rnext = (k + 1 < H) ? rot(k + 1, sg) : rot(0, -sg);
+          const float rnext = (k + 1 < H) ? rot(k + 1, ra, rb) : rot(0, na, nb);
           const float rl = 0.5f * (rcur + rnext);  // pl(p) = p+1
           const float rr = 0.5f * (rcur + rprev);  // pr(p) = p-1
           const float el = (k + 1 < H) ? es[k + 1] : esp;
@@ -208,25 +221,38 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
     float tx = 0.f, ty = 0.f;
 #pragma unroll
     for (int k = 0; k < H; ++k) {
+      // e >= 0 after every plain step (a negative e would make the reference's
+      // (e k^4)^sds_power NaN); round-off negatives after a surrogate step
+      // are cut to 0 here, which leaves every plain-path result unchanged
+      ef[k] = ef[k] < 0.f ? 0.f : ef[k];  // NaN stays NaN (the finite check must see it)
       if (valid) Eo[oS + k * 32] = ef[k];
       const float s = sin_dir(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], cp0, fkovg, tail);
       const float es_ = ef[k] * s;
       tx += es_ * prm.cth[k];
       ty += es_ * prm.sth[k];
     }
-    tx *= sg * icp;
-    ty *= sg * icp;
+    if (G == 2) {
+      tx *= ra * icp;
+      ty *= ra * icp;
+    } else {  // sums over cos/sin th0 turned into the group's frame
+      const float bx_ = tx, by_ = ty;
+      tx = (ra * bx_ - rb * by_) * icp;
+      ty = (rb * bx_ + ra * by_) * icp;
+    }
     sx += tx * kdk; sy += ty * kdk;
     if (o >= oc - 1) { dsx += tx * kdk; dsy += ty * kdk; }
     if (o == O - 1) { txom = tx; tyom = ty; }
   }
-  sx += __shfl_xor_sync(0xffffffffu, sx, 16);
-  sy += __shfl_xor_sync(0xffffffffu, sy, 16);
-  dsx += __shfl_xor_sync(0xffffffffu, dsx, 16);
-  dsy += __shfl_xor_sync(0xffffffffu, dsy, 16);
-  txom += __shfl_xor_sync(0xffffffffu, txom, 16);
-  tyom += __shfl_xor_sync(0xffffffffu, tyom, 16);
-  if (half != 0 || !valid) return;
+#pragma unroll
+  for (int m = PW; m < 32; m <<= 1) {
+    sx += __shfl_xor_sync(0xffffffffu, sx, m);
+    sy += __shfl_xor_sync(0xffffffffu, sy, m);
+    dsx += __shfl_xor_sync(0xffffffffu, dsx, m);
+    dsy += __shfl_xor_sync(0xffffffffu, dsy, m);
+    txom += __shfl_xor_sync(0xffffffffu, txom, m);
+    tyom += __shfl_xor_sync(0xffffffffu, tyom, m);
+  }
+  if (q != 0 || !valid) return;
   // ---- stress('atm') per point, umwm_stress.F90:216-262
   const float rhow = P.rhow[ja], rhoa = P.rhoa[ja], wspd = wi.wspd;
   const float kom = __ldg(P.TAB + (size_t)(O - 1) * tstride + tS + T_K * 32);
@@ -264,13 +290,28 @@ __global__ void __launch_bounds__(128, 3) k_advect(const Params prm, const Ptrs 
 }
 
 cudaError_t launch_advect(const Params& prm, const Ptrs& P, cudaStream_t st) {
-  dim3 grid(prm.ntiles), block(128);
+  const dim3 block(128);
   const bool curv = prm.curvilinear != 0;
+  if (prm.groups4 && quarter_groups(prm.P)) {
+    const dim3 grid(prm.ntiles * (TILE / 32));  // 32 points per CTA
+    switch (prm.P / 4) {
+#define CASE(X)                                                          \
+  case X:                                                                \
+    if (curv) k_advect<4, X, true><<<grid, block, 0, st>>>(prm, P);      \
+    else k_advect<4, X, false><<<grid, block, 0, st>>>(prm, P);          \
+    break;
+      CASE(4) CASE(6) CASE(8) CASE(9) CASE(12)
+#undef CASE
+      default: return cudaErrorInvalidConfiguration;
+    }
+    return cudaGetLastError();
+  }
+  const dim3 grid(prm.ntiles);  // 64 points per CTA
   switch (prm.P / 2) {
 #define CASE(X)                                                          \
   case X:                                                                \
-    if (curv) k_advect<X, true><<<grid, block, 0, st>>>(prm, P);         \
-    else k_advect<X, false><<<grid, block, 0, st>>>(prm, P);             \
+    if (curv) k_advect<2, X, true><<<grid, block, 0, st>>>(prm, P);      \
+    else k_advect<2, X, false><<<grid, block, 0, st>>>(prm, P);          \
     break;
     CASE(4) CASE(6) CASE(8) CASE(12) CASE(16) CASE(18) CASE(24)
 #undef CASE

@@ -1,13 +1,17 @@
 // Source-term kernels: sin_d12, sds_d12, snl_d12, s_ice and source()
 // (umwm_source_functions.F90:16-183, umwm_physics.F90:9-86).
 //
-// Thread mapping.  A warp owns 16 consecutive wet points; lane = point +
-// 16 * half, where half 0 takes directions p = 0..H-1 and half 1 takes
-// p = H..2H-1 (H = pm/2).  Direction p+H is direction p turned by pi, so
-// cos/sin(th) flip sign and cos/sin(2 th) are equal: both halves run the same
-// code with the direction index k = 0..H-1 known at compile time (every
-// direction constant is an immediate operand), with a per-lane sign.  Both
-// halves of a point combine their partial sums with one shuffle.
+// Thread mapping.  The pm directions of a point are split into G groups of
+// H = pm/G consecutive directions (G = 4 when pm/4 is a supported group size,
+// else G = 2); a warp owns 32/G consecutive wet points and lane = point +
+// (32/G) * q, where group q takes directions p = qH .. qH+H-1.  Group q is the
+// base group 0 turned by q*2pi/G (a quarter turn for G = 4, a half turn for
+// G = 2), so every group runs the same code with the direction index
+// k = 0..H-1 known at compile time (every direction constant of the base
+// group is a constant-bank operand) and a per-lane rotation (ra, rb):
+// cos th = ra cos th0 - rb sin th0, sin th = rb cos th0 + ra sin th0, and
+// cos/sin 2th pick up the sign cos(2 q 2pi/G).  The groups of a point combine
+// their partial sums with log2(G) shuffles.
 //
 // The frequency loop walks o = 1..om in order because the mean-square-slope
 // adjustment of Sds is a prefix over o:
@@ -31,7 +35,7 @@
 
 namespace umwm {
 
-constexpr int PTS = TILE;  // wet points per CTA (4 warps x 16)
+
 
 // bulk prefetch of a contiguous, 16-byte aligned range into L2 (sizes are multiples of 16 bytes)
 __device__ __forceinline__ void bulk_prefetch_l2(const void* p, unsigned bytes) {
@@ -94,22 +98,29 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
   return s;
 }
 
-template <int H, bool INTEG>
-__global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm, const Ptrs P, int compute_rot) {
+template <int G, int H, bool INTEG>
+__global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? 3 : 4))
+    k_source(const Params prm, const Ptrs P, int compute_rot) {
+  constexpr int PW = 32 / G;   // points per warp
+  constexpr int PPC = 4 * PW;  // points per CTA (4 warps)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int j16 = lane & 15, half = lane >> 4;
+  const int jl = lane % PW, q = lane / PW;
   const int O = prm.O;
-  const Member& Mb = prm.mem[prm.tile_mem[blockIdx.x]];
+  const int tile = (blockIdx.x * PPC) / TILE;
+  const Member& Mb = prm.mem[prm.tile_mem[tile]];
   Ctl* ctl = Mb.ctl;
   // members that have finished the current dtg sit the substep out
   if (INTEG ? !ctl->running : ctl->done) return;
-  if (INTEG && P.fb_tile && !P.fb_tile[blockIdx.x]) return;  // surrogate fallback: flagged tiles only
+  if (INTEG && P.fb_tile && !P.fb_tile[tile]) return;  // surrogate fallback: flagged tiles only
   const int N = Mb.ghost;  // this member's ghost point (its wet points end here)
-  const int j = blockIdx.x * PTS + w * 16 + j16;
+  const int j = blockIdx.x * PPC + w * PW + jl;
   const bool valid = j < N && (!INTEG || !P.fb_pt || P.fb_pt[j]);
   const int jj = valid ? j : N;  // the ghost keeps loads in bounds
   const int ja = apt(Mb, jj);
-  const float sg = half ? -1.f : 1.f;
+  // rotation of this lane's group relative to the base group
+  const float ra = G == 2 ? (q ? -1.f : 1.f) : (q == 0 ? 1.f : (q == 2 ? -1.f : 0.f));
+  const float rb = G == 2 ? 0.f : (q == 1 ? 1.f : (q == 3 ? -1.f : 0.f));
+  const float c2s = (G == 4 && (q & 1)) ? -1.f : 1.f;  // cos/sin(2 th) sign of the group
   __shared__ float cws[H][128];
 
   const float dts = INTEG ? ctl->dts : 0.f;
@@ -119,9 +130,11 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
   const float sdtc = (prm.sdt_fac * sqrtf(P.rhorat[ja])) * ustar;
   const float sv = prm.ice_possible ? P.sice_v[jj] : 0.f;
   const float hdth = 0.5f * prm.dth;
-  const float ucg = sg * wi.uc, vcg = sg * wi.vc;
+  // currents in the group's frame: uc cos th + vc sin th = ucg cos th0 + vcg sin th0
+  const float ucg = G == 2 ? ra * wi.uc : ra * wi.uc + rb * wi.vc;
+  const float vcg = G == 2 ? ra * wi.vc : ra * wi.vc - rb * wi.uc;
 #pragma unroll
-  for (int k = 0; k < H; ++k) cws[k][threadIdx.x] = cosf(wdir - prm.th[half * H + k]);
+  for (int k = 0; k < H; ++k) cws[k][threadIdx.x] = cosf(wdir - prm.th[q * H + k]);
   // own bins only: no barrier needed (each thread reads its own column)
 
   int nie = N, niw = N, nin = N, nis = N;
@@ -135,11 +148,12 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
   // level strides of the blocked layouts
   const size_t lstride = (size_t)prm.NB * prm.P * 32;
   const size_t tstride = (size_t)prm.NB * T_COUNT * 32;
-  const float* Eb = P.E + sidx(prm, 0, half * H, jj);
+  const float* Eb = P.E + sidx(prm, 0, q * H, jj);
   const float* Tb = P.TAB + tidx(prm, 0, 0, jj);
   const float* Eblk = P.E + sidx(prm, 0, 0, jj & ~31);  // start of this block's region
   auto pf = [&](int o) {
-    if (o < O && lane == 0) bulk_prefetch_l2(Eblk + (size_t)o * lstride, (unsigned)(prm.P * 128));
+    if (o < O && lane == 0 && (G == 2 || (w * PW) % 32 == 0))
+      bulk_prefetch_l2(Eblk + (size_t)o * lstride, (unsigned)(prm.P * 128));
   };
   pf(0);
   pf(1);
@@ -161,7 +175,9 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
       for (int k = 0; k < H; ++k) ec[k] = r[k * 32];  // E is also written (as ef) by this kernel
       const bool prog = o < wi.oc;
       const Level<H> Lc = load_level<H>(prm, Tb + (size_t)o * tstride, !INTEG && prog);
-      Cc.a = A; Cc.b = B; Cc.c = C;
+      // the group's cos/sin 2th sign folded into the coefficients
+      const float Bq = G == 4 ? c2s * B : B, Cq = G == 4 ? c2s * C : C;
+      Cc.a = A; Cc.b = Bq; Cc.c = Cq;
       float s0 = 0.f, sc2 = 0.f, ss2 = 0.f;
 #pragma unroll
       for (int k = 0; k < H; ++k) {
@@ -169,14 +185,21 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
         sc2 += ec[k] * prm.c2th[k];
         ss2 += ec[k] * prm.s2th[k];
       }
-      s0 += __shfl_xor_sync(0xffffffffu, s0, 16);
-      sc2 += __shfl_xor_sync(0xffffffffu, sc2, 16);
-      ss2 += __shfl_xor_sync(0xffffffffu, ss2, 16);
+      if (G == 4) {
+        sc2 *= c2s;
+        ss2 *= c2s;
+      }
+#pragma unroll
+      for (int m = PW; m < 32; m <<= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, m);
+        sc2 += __shfl_xor_sync(0xffffffffu, sc2, m);
+        ss2 += __shfl_xor_sync(0xffffffffu, ss2, m);
+      }
       const float sA = prm.twopisds_fac * prm.f[o];
       if (INTEG || prog) {
 #pragma unroll
         for (int k = 0; k < H; ++k) {
-          const float chi = A + B * prm.c2th[k] + C * prm.s2th[k];
+          const float chi = A + Bq * prm.c2th[k] + Cq * prm.s2th[k];
           const float t = 1.f + prm.mss_fac * chi;
           sc[k] = (sA * (t * t)) * powp(ec[k] * Lc.k4, prm.sds_power);
         }
@@ -196,11 +219,19 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
           const float* CP = P.TAB + (size_t)o * tstride + T_CP0 * 32;
           const float dcx = __ldg(CP + tidx(prm, 0, 0, nie)) - __ldg(CP + tidx(prm, 0, 0, niw));
           const float dcy = __ldg(CP + tidx(prm, 0, 0, nin)) - __ldg(CP + tidx(prm, 0, 0, nis));
-          const float gx = sg * dcx, gy = sg * dcy;
+          if (G == 2) {
+            const float gx = ra * dcx, gy = ra * dcy;
 #pragma unroll
-          for (int k = 0; k < H; ++k) {
-            const float rr = 0.5f * ((gx * prm.sth[k] + vce - vcw) * odx - (gy * prm.cth[k] + ucn - ucs) * ody);
-            rmx = fmaxf(rmx, rr);
+            for (int k = 0; k < H; ++k) {
+              const float rr = 0.5f * ((gx * prm.sth[k] + vce - vcw) * odx - (gy * prm.cth[k] + ucn - ucs) * ody);
+              rmx = fmaxf(rmx, rr);
+            }
+          } else {
+            // dcx sin th - dcy cos th in the group's frame
+            const float ps = 0.5f * (ra * dcx * odx + rb * dcy * ody), pc = 0.5f * (rb * dcx * odx - ra * dcy * ody);
+            const float p0 = 0.5f * ((vce - vcw) * odx - (ucn - ucs) * ody);
+#pragma unroll
+            for (int k = 0; k < H; ++k) rmx = fmaxf(rmx, ps * prm.sth[k] + pc * prm.cth[k] + p0);
           }
         }
       }
@@ -217,8 +248,8 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
       const float U = wi.wspd + wi.ustar25 * L2.logl2z;
       const float sdt = sdtc * L2.kk;
       const float sice = sv != 0.f ? 2.f * L2.cg0 * sv : 0.f;
-      float* ES = P.ES + sidx(prm, 0, half * H, jj) + (size_t)Lv * lstride;
-      float* EF = P.EF + sidx(prm, 0, half * H, jj) + (size_t)Lv * lstride;
+      float* ES = P.ES + sidx(prm, 0, q * H, jj) + (size_t)Lv * lstride;
+      float* EF = P.EF + sidx(prm, 0, q * H, jj) + (size_t)Lv * lstride;
       if (prog) {
 #pragma unroll
         for (int k = 0; k < H; ++k) {
@@ -264,12 +295,13 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
   }
 
   if (!INTEG) {
-    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 16));
+#pragma unroll
+    for (int m = PW; m < 32; m <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, m));
     float ph = prm.explim / mx;
-    if (valid && half == 0) P.phys[j] = ph;
+    if (valid && q == 0) P.phys[j] = ph;
     float bm = valid ? ph : __int_as_float(0x7f800000);
 #pragma unroll
-    for (int s = 8; s > 0; s >>= 1) bm = fminf(bm, __shfl_xor_sync(0xffffffffu, bm, s));
+    for (int s = PW / 2; s > 0; s >>= 1) bm = fminf(bm, __shfl_xor_sync(0xffffffffu, bm, s));
     if (lane == 0) atomicMin(&ctl->minphys_enc, enc_ord_d(bm));
     if (compute_rot) {
       float m = valid ? rmx : 0.f;
@@ -282,10 +314,22 @@ __global__ void __launch_bounds__(128, INTEG ? 3 : 4) k_source(const Params prm,
 
 template <bool INTEG>
 static cudaError_t launch_source_t(const Params& prm, const Ptrs& P, int compute_rot, cudaStream_t st) {
-  dim3 grid(prm.ntiles), block(128);
+  const dim3 block(128);
+  if (prm.groups4 && quarter_groups(prm.P)) {
+    const dim3 grid(prm.ntiles * (TILE / 32));  // 32 points per CTA
+    switch (prm.P / 4) {
+#define CASE(X) \
+  case X: k_source<4, X, INTEG><<<grid, block, 0, st>>>(prm, P, compute_rot); break;
+      CASE(4) CASE(6) CASE(8) CASE(9) CASE(12)
+#undef CASE
+      default: return cudaErrorInvalidConfiguration;
+    }
+    return cudaGetLastError();
+  }
+  const dim3 grid(prm.ntiles);  // 64 points per CTA
   switch (prm.P / 2) {
 #define CASE(X) \
-  case X: k_source<X, INTEG><<<grid, block, 0, st>>>(prm, P, compute_rot); break;
+  case X: k_source<2, X, INTEG><<<grid, block, 0, st>>>(prm, P, compute_rot); break;
     CASE(4) CASE(6) CASE(8) CASE(12) CASE(16) CASE(18) CASE(24)
 #undef CASE
     default: return cudaErrorInvalidConfiguration;

@@ -35,7 +35,22 @@ __device__ __forceinline__ PointInfo point_info(const Params& prm, const Ptrs& P
   return q;
 }
 
-__device__ __forceinline__ float feature(float e) { return (logf(e + EPS) - LN_C0) * (1.f / LN_C1); }
+__device__ __forceinline__ float feature(float e) { return (logf(fmaxf(e, 0.f) + EPS) - LN_C0) * (1.f / LN_C1); }
+
+// Surrogate step of one bin: the predicted log-tendency, capped above by the
+// growth the wind input allows over dts (dts * max(Sin, 0) + GROWTH_SLACK).
+// Without wind input a bin cannot grow in the plain step, so the cap stops a
+// network error from feeding energy into bins the forcing does not reach.
+constexpr float GROWTH_SLACK = 0.02f;
+__device__ __forceinline__ float step_bin(const Params& prm, const Ptrs& P, const WindIn& wi, float dts, float wdir,
+                                          float e, float y, int o, int p, int j, float& sin_pos) {
+  const float* T = P.TAB + tidx(prm, o, 0, j);
+  const float sin_ = sin_bin(prm, wi, cosf(wdir - prm.th[p]), prm.cth[p], prm.sth[p], T[T_LOGL2Z * 32],
+                             T[T_CP0 * 32], T[T_FKOVG * 32], o >= wi.oc);
+  sin_pos = fmaxf(sin_, 0.f);
+  const float d = fminf(TS * y, dts * sin_pos + GROWTH_SLACK);
+  return fmaxf((fmaxf(e, 0.f) + EPS) * expf(d) - EPS, 0.f);
+}
 
 __device__ __forceinline__ __nv_bfloat16* row_h(uint32_t* tile, int r) {
   return reinterpret_cast<__nv_bfloat16*>(tile + r * PITCHW);
@@ -111,17 +126,25 @@ __global__ void k_targets(const Params prm, const Ptrs P, const int* pts, int n,
       int p = pr + s;
       if (p >= NP) p -= NP;
       const float ef = P.EF[sidx(prm, o, p, pts[r])];
-      t = (logf(ef + EPS) - logf(ecopy[(size_t)r * F0 + c] + EPS)) * (1.f / TS);
+      t = (logf(fmaxf(ef, 0.f) + EPS) - logf(fmaxf(ecopy[(size_t)r * F0 + c], 0.f) + EPS)) * (1.f / TS);
     }
     T[idx] = __float2bfloat16_rn(t);
   }
 }
 
 __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, const __nv_bfloat16* Y, float tol,
-                                               unsigned char* fb_pt, int* fb_tile, unsigned long long* counts) {
+                                               float tol_level, unsigned char* fb_pt, int* fb_tile,
+                                               unsigned long long* counts) {
   extern __shared__ uint32_t tile[];
-  __shared__ float red0[8][32], red1[8][32];
+  __shared__ float red0[8][32], red1[8][32], red2[8][32], red3[8][32];
+  __shared__ float lev0[MAX_OM][32], lev1[MAX_OM][32];  // energy of each frequency level before / after
   __shared__ int s_ok[32], s_s[32], s_pass[32];
+  __shared__ WindIn s_wi[32];
+  __shared__ float s_wdir[32], s_dts[32];
+  for (int i = threadIdx.x; i < MAX_OM * 32; i += blockDim.x) {
+    (&lev0[0][0])[i] = 0.f;
+    (&lev1[0][0])[i] = 0.f;
+  }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int jb = blockIdx.x, j = jb * 32 + lane;
   const int NP = prm.P, F0 = prm.O * prm.P;
@@ -129,6 +152,12 @@ __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, c
     const PointInfo q = point_info(prm, P, j);
     s_ok[lane] = q.ok;
     s_s[lane] = q.s;
+    if (q.ok) {
+      const Member& M = prm.mem[prm.tile_mem[j / TILE]];
+      s_wi[lane] = load_wind(prm, P, j, apt(M, j), P.ustar[j]);
+      s_wdir[lane] = q.psi;
+      s_dts[lane] = M.ctl->dts;
+    }
   }
   const uint32_t* Y32 = reinterpret_cast<const uint32_t*>(Y);
   for (int rr = warp; rr < 32; rr += 8)
@@ -136,29 +165,53 @@ __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, c
   __syncthreads();
   const int ok = s_ok[lane], s = s_s[lane];
   const __nv_bfloat16* h = row_h(tile, lane);
-  float m0 = 0.f, m1 = 0.f;
+  const WindIn wi = s_wi[lane];
+  const float wdir = s_wdir[lane], dts = s_dts[lane];
+  float m0 = 0.f, m1 = 0.f, w0 = 0.f, w1 = 0.f;  // energy, and energy where the wind feeds (weight Sin)
   if (ok) {
     for (int b = warp; b < F0; b += 8) {
       const int o = b / NP, p = b - o * NP;
       int pr = p - s;
       if (pr < 0) pr += NP;
       const float e = P.E[sidx(prm, o, p, j)];
-      const float ef = fmaxf((e + EPS) * expf(TS * __bfloat162float(h[o * NP + pr])) - EPS, 0.f);
+      float sp;
+      const float ef = step_bin(prm, P, wi, dts, wdir, e, __bfloat162float(h[o * NP + pr]), o, p, j, sp);
       const float kdk = P.TAB[tidx(prm, o, T_KDK, j)];
       m0 += e * kdk;
       m1 += ef * kdk;
+      w0 += fmaxf(e, 0.f) * sp * kdk;
+      w1 += ef * sp * kdk;
+      atomicAdd(&lev0[o][lane], fmaxf(e, 0.f));
+      atomicAdd(&lev1[o][lane], ef);
     }
   }
   red0[warp][lane] = m0;
   red1[warp][lane] = m1;
+  red2[warp][lane] = w0;
+  red3[warp][lane] = w1;
   __syncthreads();
   if (warp == 0) {
-    float a = 0.f, b = 0.f;
+    float a = 0.f, b = 0.f, wa = 0.f, wb = 0.f;
     for (int w = 0; w < 8; ++w) {
       a += red0[w][lane];
       b += red1[w][lane];
+      wa += red2[w][lane];
+      wb += red3[w][lane];
     }
-    const bool pass = ok && isfinite(b) && fabsf(logf((b + 1e-30f) / (a + 1e-30f))) <= tol;
+    // total energy (sum e k dk, as Hs^2) within tol, and every frequency
+    // level holding more than 1e-4 of the largest level's energy within
+    // tol_level (the total alone hardly sees the low frequencies)
+    // the wind-weighted energy (sum e max(Sin,0) k dk, which sets the form
+    // stress and so ustar) within tol_level as well
+    bool pass = ok && isfinite(b) && fabsf(logf((b + 1e-30f) / (a + 1e-30f))) <= tol &&
+                isfinite(wb) && fabsf(logf((wb + 1e-30f) / (wa + 1e-30f))) <= tol_level;
+    if (pass) {
+      float lmax = 0.f;
+      for (int o = 0; o < prm.O; ++o) lmax = fmaxf(lmax, lev0[o][lane]);
+      const float floor_ = 1e-4f * lmax + 1e-30f;
+      for (int o = 0; o < prm.O; ++o)
+        if (!(fabsf(logf((lev1[o][lane] + floor_) / (lev0[o][lane] + floor_))) <= tol_level)) pass = false;
+    }
     s_pass[lane] = pass ? 1 : 0;
     if (j < prm.Ntot) fb_pt[j] = (ok && !pass) ? 1 : 0;
     const unsigned fails = __ballot_sync(0xffffffffu, ok && !pass);
@@ -177,7 +230,8 @@ __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, c
     if (pr < 0) pr += NP;
     const size_t k = sidx(prm, o, p, j);
     const float e = P.E[k];
-    const float ef = fmaxf((e + EPS) * expf(TS * __bfloat162float(h[o * NP + pr])) - EPS, 0.f);
+    float sp;
+    const float ef = step_bin(prm, P, wi, dts, wdir, e, __bfloat162float(h[o * NP + pr]), o, p, j, sp);
     P.ES[k] = 0.5f * (e + ef);
     P.EF[k] = ef;
   }
@@ -285,11 +339,11 @@ cudaError_t launch_targets(const Params& prm, const Ptrs& P, const int* pts, int
   return cudaGetLastError();
 }
 
-cudaError_t launch_apply(const Params& prm, const Ptrs& P, const __nv_bfloat16* Y, float tol, unsigned char* fb_pt,
-                         int* fb_tile, unsigned long long* counts, cudaStream_t st) {
+cudaError_t launch_apply(const Params& prm, const Ptrs& P, const __nv_bfloat16* Y, float tol, float tol_level,
+                         unsigned char* fb_pt, int* fb_tile, unsigned long long* counts, cudaStream_t st) {
   static cudaError_t attr = cudaFuncSetAttribute(k_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_SMEM);
   if (attr != cudaSuccess) return attr;
-  k_apply<<<prm.NB, 256, TILE_SMEM, st>>>(prm, P, Y, tol, fb_pt, fb_tile, counts);
+  k_apply<<<prm.NB, 256, TILE_SMEM, st>>>(prm, P, Y, tol, tol_level, fb_pt, fb_tile, counts);
   return cudaGetLastError();
 }
 

@@ -65,6 +65,7 @@ struct State {
   // pair store
   DevBuf sX, sT;
   long cap = 0, count = 0;
+  long holdout = 0;  // trailing stored pairs kept out of training
   int per_substep = 0;
   bool capture_on = false;
   DevBuf c_pts, c_shift, c_ecopy;
@@ -73,9 +74,17 @@ struct State {
   uint64_t rng = 0x9e3779b97f4a7c15ull;
   // inference inside the model
   bool active = false;
-  float tol = 0.1f;
+  float tol = 0.02f;        // total-energy budget per substep (ln)
+  float tol_level = 0.1f;   // per-level energy budget per substep (ln)
   DevBuf iX, iH1, iH2, fb_pt, fb_tile, counts;
   unsigned long long applied = 0, fallback = 0;
+  // per-stage CUDA-event timing of the surrogate step (option "surrogate_timing")
+  bool timing = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool ev_pending = false;
+  double ms_features = 0, ms_gemm = 0, ms_apply = 0;
+  long long timed_steps = 0;
+  long long rows_gemm = 0;
   // training batch buffers
   DevBuf bX, bT, Z1, H1, Z2, H2, Yf, dY, dZ2, dZ1, dYt, H2t, dZ2t, H1t, dZ1t, Xt, bidx, loss;
 };
@@ -215,6 +224,22 @@ int backward(int B, float* dloss, cudaStream_t st) {
   return UMWM_OK;
 }
 
+// accumulate the stage times of the last timed step (its events are complete
+// once the stream has been synchronised)
+void collect_timing() {
+  if (!S.ev_pending) return;
+  if (cudaEventSynchronize(S.ev[3]) != cudaSuccess) return;
+  float a = 0, b = 0, c = 0;
+  cudaEventElapsedTime(&a, S.ev[0], S.ev[1]);
+  cudaEventElapsedTime(&b, S.ev[1], S.ev[2]);
+  cudaEventElapsedTime(&c, S.ev[2], S.ev[3]);
+  S.ms_features += a;
+  S.ms_gemm += b;
+  S.ms_apply += c;
+  S.timed_steps += 1;
+  S.ev_pending = false;
+}
+
 int need_init() {
   if (!S.init) return set_error(UMWM_ERR_STATE, "surrogate: call umwm_gpu_surrogate_init first");
   return UMWM_OK;
@@ -277,14 +302,28 @@ int step(const Params& prm, const Ptrs& P, Ptrs& fbP, cudaStream_t st) {
   SCU(S.iH2.ensure(n * HID * 2));
   SCU(S.fb_pt.ensure(n));
   SCU(S.fb_tile.ensure((size_t)prm.ntiles * 4));
-  SCU(S.counts.ensure(2 * sizeof(unsigned long long)));
+  if (!S.counts.p) {
+    SCU(S.counts.ensure(2 * sizeof(unsigned long long)));
+    SCU(cudaMemsetAsync(S.counts.p, 0, 2 * sizeof(unsigned long long), st));
+  }
+  collect_timing();
+  if (S.timing && !S.ev[0])
+    for (cudaEvent_t& e : S.ev) SCU(cudaEventCreate(&e));
+  if (S.timing) SCU(cudaEventRecord(S.ev[0], st));
   SCU(launch_features(prm, P, nullptr, (int)n, S.iX.as<bf16>(), nullptr, nullptr, st));
+  if (S.timing) SCU(cudaEventRecord(S.ev[1], st));
   int rc = forward(S.iX.as<bf16>(), (int)n, S.iH1.as<bf16>(), S.iH2.as<bf16>(), nullptr, nullptr, nullptr,
                    S.iX.as<bf16>(), st);  // outputs overwrite the inputs
   if (rc) return rc;
+  if (S.timing) SCU(cudaEventRecord(S.ev[2], st));
   SCU(cudaMemsetAsync(S.fb_tile.p, 0, (size_t)prm.ntiles * 4, st));
-  SCU(launch_apply(prm, P, S.iX.as<bf16>(), S.tol, S.fb_pt.as<unsigned char>(), S.fb_tile.as<int>(),
+  SCU(launch_apply(prm, P, S.iX.as<bf16>(), S.tol, S.tol_level, S.fb_pt.as<unsigned char>(), S.fb_tile.as<int>(),
                    S.counts.as<unsigned long long>(), st));
+  if (S.timing) {
+    SCU(cudaEventRecord(S.ev[3], st));
+    S.ev_pending = true;
+    S.rows_gemm = (long long)n;
+  }
   fbP = P;
   fbP.fb_tile = S.fb_tile.as<int>();
   fbP.fb_pt = S.fb_pt.as<unsigned char>();
@@ -301,6 +340,23 @@ int set_option(const std::string& name, double value) {
     S.active = value != 0;
     return UMWM_OK;
   }
+  if (name == "surrogate_timing") {
+    collect_timing();
+    S.timing = value != 0;
+    S.ms_features = S.ms_gemm = S.ms_apply = 0;
+    S.timed_steps = 0;
+    return UMWM_OK;
+  }
+  if (name == "surrogate_holdout") {
+    if (value < 0) return set_error(UMWM_ERR_ARG, "surrogate_holdout must be >= 0");
+    S.holdout = (long)value;
+    return UMWM_OK;
+  }
+  if (name == "surrogate_tol_level") {
+    if (!(value > 0)) return set_error(UMWM_ERR_ARG, "surrogate_tol_level must be > 0");
+    S.tol_level = (float)value;
+    return UMWM_OK;
+  }
   if (name == "surrogate_tol") {
     if (!(value > 0)) return set_error(UMWM_ERR_ARG, "surrogate_tol must be > 0");
     S.tol = (float)value;
@@ -313,6 +369,14 @@ double get_stat(const std::string& name) {
   if (name == "surrogate_nparams") return (double)NPARAM;
   if (name == "surrogate_pairs") return (double)S.count;
   if (name == "surrogate_width") return (double)FPAD;
+  if (name.compare(0, 13, "surrogate_ms_") == 0 || name == "surrogate_timed_steps" || name == "surrogate_rows") {
+    collect_timing();
+    if (name == "surrogate_ms_features") return S.ms_features;
+    if (name == "surrogate_ms_gemm") return S.ms_gemm;
+    if (name == "surrogate_ms_apply") return S.ms_apply;
+    if (name == "surrogate_rows") return (double)S.rows_gemm;
+    return (double)S.timed_steps;
+  }
   if (name == "surrogate_points" || name == "surrogate_fallback") {
     if (S.counts.p) {
       unsigned long long c[2] = {0, 0};
@@ -410,7 +474,8 @@ int umwm_gpu_surrogate_train(int steps, int batch, double lr, unsigned long long
   int rc = need_init();
   if (rc) return rc;
   if (steps <= 0 || batch <= 0 || batch % 128) return set_error(UMWM_ERR_ARG, "surrogate_train: batch % 128 != 0");
-  if (S.count < batch) return set_error(UMWM_ERR_STATE, "surrogate_train: fewer captured pairs than one batch");
+  const long ntrain = S.count - std::min(S.holdout, S.count);
+  if (ntrain < batch) return set_error(UMWM_ERR_STATE, "surrogate_train: fewer training pairs than one batch");
   if ((rc = ensure_batch(batch))) return rc;
   SCU(S.bidx.ensure((size_t)batch * 4));
   DevBuf dl;
@@ -427,7 +492,7 @@ int umwm_gpu_surrogate_train(int steps, int batch, double lr, unsigned long long
       cudaError_t e = cudaStreamSynchronize(S.st);
       if (e != cudaSuccess) { rc = cuda_fail(e, "train sync"); break; }
     }
-    for (int i = 0; i < batch; ++i) hb[i] = (int)std::min<long>((long)(uniform(r) * S.count), S.count - 1);
+    for (int i = 0; i < batch; ++i) hb[i] = (int)std::min<long>((long)(uniform(r) * ntrain), ntrain - 1);
     cudaError_t e = cudaMemcpyAsync(S.bidx.p, hb, (size_t)batch * 4, cudaMemcpyHostToDevice, S.st);
     if (e == cudaSuccess) e = launch_gather_rows(S.sX.as<bf16>(), S.bidx.as<int>(), batch, FPAD, S.bX.as<bf16>(), S.st);
     if (e == cudaSuccess) e = launch_gather_rows(S.sT.as<bf16>(), S.bidx.as<int>(), batch, FPAD, S.bT.as<bf16>(), S.st);
@@ -448,6 +513,39 @@ int umwm_gpu_surrogate_train(int steps, int batch, double lr, unsigned long long
   if (losses) SCU(cudaMemcpy(losses, dl.p, (size_t)steps * 4, cudaMemcpyDeviceToHost));
   dl.release();
   return UMWM_OK;
+}
+
+int umwm_gpu_surrogate_eval(long first, long count, double* loss) {
+  int rc = need_init();
+  if (rc) return rc;
+  if (!loss || first < 0 || count <= 0 || first + count > S.count)
+    return set_error(UMWM_ERR_ARG, "surrogate_eval: rows outside the stored pairs");
+  const int B = 8192;
+  if ((rc = ensure_batch(B))) return rc;
+  DevBuf dl, idx;
+  const long nb = (count + B - 1) / B;
+  SCU(dl.ensure((size_t)nb * 4));
+  SCU(idx.ensure((size_t)B * 4));
+  SCU(cudaMemsetAsync(dl.p, 0, (size_t)nb * 4, S.st));
+  std::vector<int> h(B);
+  for (long b = 0; b < nb; ++b) {
+    const int n = (int)std::min<long>(B, count - b * B);
+    for (int i = 0; i < n; ++i) h[i] = (int)(first + b * B + i);
+    SCU(cudaMemcpyAsync(idx.p, h.data(), (size_t)n * 4, cudaMemcpyHostToDevice, S.st));
+    SCU(launch_gather_rows(S.sX.as<bf16>(), idx.as<int>(), n, FPAD, S.bX.as<bf16>(), S.st));
+    SCU(launch_gather_rows(S.sT.as<bf16>(), idx.as<int>(), n, FPAD, S.bT.as<bf16>(), S.st));
+    if ((rc = forward(S.bX.as<bf16>(), n, S.H1.as<bf16>(), S.H2.as<bf16>(), S.Z1.as<bf16>(), S.Z2.as<bf16>(),
+                      S.Yf.as<float>(), nullptr, S.st)))
+      return rc;
+    SCU(launch_loss(S.Yf.as<float>(), S.bT.as<bf16>(), n, S.F0, S.dY.as<bf16>(), dl.as<float>() + b, S.st));
+    SCU(cudaStreamSynchronize(S.st));  // h is reused
+  }
+  std::vector<float> l(nb);
+  SCU(cudaMemcpy(l.data(), dl.p, (size_t)nb * 4, cudaMemcpyDeviceToHost));
+  double acc = 0;
+  for (long b = 0; b < nb; ++b) acc += (double)l[b] * std::min<long>(B, count - b * B);
+  *loss = acc / count;
+  return check_err();
 }
 
 int umwm_gpu_surrogate_forward(const float* X, int n, float* Y) {

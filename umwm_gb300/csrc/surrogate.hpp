@@ -16,8 +16,10 @@
 //   x[F0 + 6] = current across      x[F0 + 7] = rhoa / rhow * 800
 //   x[F0 + 8] = fice                the rest zero (F0 = om*pm)
 // Output y (width FPAD, first F0 used) in the same rotated frame:
-//   ef = max((e + EPS) exp(TS * y) - EPS, 0),   ES = (e + ef) / 2,   EF = ef
-// i.e. the step the plain path takes in umwm_physics.F90:61-84.
+//   ef = max((e + EPS) exp(min(TS * y, dts max(Sin, 0) + 0.02)) - EPS, 0),
+//   ES = (e + ef) / 2,   EF = ef
+// i.e. the step the plain path takes in umwm_physics.F90:61-84, with growth
+// capped by the bin's wind input Sin (sin_d12, umwm_source_functions.F90:39-80).
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -52,10 +54,12 @@ cudaError_t launch_features(const Params& prm, const Ptrs& P, const int* pts, in
 cudaError_t launch_targets(const Params& prm, const Ptrs& P, const int* pts, int n, const float* ecopy,
                            const int* shift, __nv_bfloat16* T, cudaStream_t st);
 // Apply the predicted step (Y: ldN x FPAD bf16) to every running wet point
-// whose energy budget passes: |ln(m1/m0)| <= tol, m = sum e k dk.  Failing
-// points get fb_pt[j] = 1 and their tile fb_tile[t] = 1 and keep e; counts
-// [0] += points applied, [1] += points failing.
-cudaError_t launch_apply(const Params& prm, const Ptrs& P, const __nv_bfloat16* Y, float tol,
+// whose energy budget passes: |ln(m1/m0)| <= tol, m = sum e k dk, and for
+// every frequency level o holding more than 1e-4 of the point's largest
+// level energy, |ln(L1_o/L0_o)| <= tol_level, L_o = sum_p e.  Failing points
+// get fb_pt[j] = 1 and their tile fb_tile[t] = 1 and keep e; counts[0] +=
+// points applied, [1] += points failing.
+cudaError_t launch_apply(const Params& prm, const Ptrs& P, const __nv_bfloat16* Y, float tol, float tol_level,
                          unsigned char* fb_pt, int* fb_tile, unsigned long long* counts, cudaStream_t st);
 
 // training helpers

@@ -1250,6 +1250,16 @@ int umwm_gpu_set_option(const char* name, double value) {
   if (s == "max_substeps") { M->max_substeps = (long long)value; return UMWM_OK; }
   if (s == "check_finite") { M->check_finite = value != 0; return UMWM_OK; }
   if (s == "use_graph") { M->use_graph = value != 0; return UMWM_OK; }
+  if (s == "direction_groups") {
+    if (value != 2 && value != 4) return fail(UMWM_ERR_ARG, "direction_groups must be 2 or 4");
+    if (value == 4 && !quarter_groups(M->prm.P))
+      return fail(UMWM_ERR_UNSUPPORTED, "direction_groups 4 needs pm % 4 == 0 and pm/4 in {4, 6, 8, 9, 12}");
+    M->prm.groups4 = value == 4 ? 1 : 0;
+    // the captured inner loop holds the old launch configuration
+    if (M->graph_exec) { cudaGraphExecDestroy(M->graph_exec); M->graph_exec = nullptr; }
+    if (M->graph) { cudaGraphDestroy(M->graph); M->graph = nullptr; }
+    return UMWM_OK;
+  }
   return fail(UMWM_ERR_ARG, "set_option: unknown option " + s);
 }
 

@@ -248,6 +248,13 @@ def surrogate_train(steps, batch=4096, lr=1e-3, seed=0):
     return losses
 
 
+def surrogate_eval(first, count):
+    """Mean-squared-error loss of the network over stored pairs [first, first+count)."""
+    out = ctypes.c_double(0)
+    check(lib().umwm_gpu_surrogate_eval(int(first), int(count), ctypes.byref(out)))
+    return out.value
+
+
 def surrogate_forward(X):
     X = _f32(X)
     n = X.shape[0]
