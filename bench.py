@@ -21,6 +21,7 @@ host cores on a bounded crop of the same workload.
 import argparse
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -189,11 +190,16 @@ def run_reference(args):
     rank, world, _ = rank_info()
     if rank != 0:
         return 0
-    threads = os.cpu_count() or 1
+    threads = args.cpu_threads or os.cpu_count() or 1
     from oracle import pyoracle
     from umwm_gb300 import configs
 
-    case = configs.random_field(mm=args.ref_size, nm=args.ref_size, hours=3)
+    if args.case == "hurricane":
+        case = configs.hurricane(mm=args.ref_size, nm=args.ref_size, hours=12, seed=3)
+    elif args.case == "fetch_limited":
+        case = configs.fetch_limited(mm=args.ref_size, nm=args.ref_size, hours=6)
+    else:
+        case = configs.random_field(mm=args.ref_size, nm=args.ref_size, hours=3)
     nt = pyoracle.set_threads(threads)
     o = pyoracle.Oracle(case.nml, 32)
     case.stage(o)
@@ -214,12 +220,12 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": "random_field %dx%d crop of the 1000x1000 workload (%d wet points)"
-                                   % (args.ref_size, args.ref_size, im), "wet_points": im, "bins_per_point": BINS},
+            "config": {"workload": "%s %dx%d (%d wet points)" % (args.case, args.ref_size, args.ref_size, im),
+                       "wet_points": im, "bins_per_point": BINS},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port",
-                             "sample": "%d substeps of a %dx%d crop, fp32 oracle (CPU restatement of the reference;"
+                             "sample": "%d substeps of %s %dx%d, fp32 oracle (CPU restatement of the reference;"
                                        " the Fortran reference cannot be built: no Fortran compiler or netCDF)"
-                                       % (args.steps, args.ref_size, args.ref_size)},
+                                       % (args.steps, args.case, args.ref_size, args.ref_size)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -370,8 +376,29 @@ def run_surrogate(args):
         U.set_option("surrogate", 1 if sur else 0)
         U.set_option("surrogate_timing", 1 if sur else 0)
         p0, f0 = U.stat("surrogate_points"), U.stat("surrogate_fallback")
-        U.umwm_run(ev.start, ev.stop)
-        out = {"gpu_ms": U.stat("gpu_ms"), "bins": U.stat("bin_updates"), "substeps": U.dims()["substeps"],
+        gpu_ms = bins = 0.0
+        hourly = []
+        stopped = None
+        if sur:
+            # a diverging run stops at the first non-finite Hs/ustar, or when it
+            # needs more than three times the plain run's substeps
+            U.set_option("check_finite", 1)
+            U.set_option("max_substeps", 3 * plain_substeps)
+        for h in range(int(args.hours)):  # hour by hour: Hs after every hour
+            try:
+                U.umwm_run(configs._time_str(ev.start, 3600 * h), configs._time_str(ev.start, 3600 * (h + 1)))
+            except U.UmwmError as exc:
+                stopped = {"hour": h, "reason": str(exc)}
+                break
+            gpu_ms += U.stat("gpu_ms")
+            bins += U.stat("bin_updates")
+            hourly.append(U.get_field("ht").astype(np.float64))
+            if sur and U.dims()["substeps"] >= 3 * plain_substeps:
+                stopped = {"hour": h + 1, "reason": "more than 3x the plain run's substeps"}
+                break
+        U.set_option("check_finite", 0)
+        U.set_option("max_substeps", -1)
+        out = {"gpu_ms": gpu_ms, "bins": bins, "substeps": U.dims()["substeps"], "hourly": hourly, "stopped": stopped,
                "ht": U.get_field("ht"), "dwp": U.get_field("dwp"), "mwd": U.get_field("mwd"),
                "points": U.stat("surrogate_points") - p0, "fallback": U.stat("surrogate_fallback") - f0}
         if sur:
@@ -382,19 +409,36 @@ def run_surrogate(args):
         U.umwm_finalize()
         return out
 
+    plain_substeps = 10 ** 9
     plain = run(False)
+    plain_substeps = plain["substeps"]
     sur = run(True)
-    hp, hs = plain["ht"].astype(np.float64), sur["ht"].astype(np.float64)
-    wet = hp > 1e-3
-    hs_err = {"mean_abs_rel": float(np.abs(hs - hp)[wet].mean() / hp[wet].mean()),
-              "rel_l2": float(np.linalg.norm((hs - hp)[wet]) / np.linalg.norm(hp[wet])),
-              "p99_rel": float(np.percentile(np.abs(hs - hp)[wet] / hp[wet], 99)),
-              "domain_mean_rel": float(abs(hs[wet].mean() - hp[wet].mean()) / hp[wet].mean())}
-    tp_err = {"mean_abs_rel": float((np.abs(sur["dwp"] - plain["dwp"])[wet] / plain["dwp"][wet]).mean()),
-              "same_bin_frac": float((sur["dwp"] == plain["dwp"])[wet].mean())}
-    dir_err = {"mean_abs_deg": float(_angle_err_deg(sur["mwd"], plain["mwd"])[wet].mean()),
-               "hs_weighted_deg": float((_angle_err_deg(sur["mwd"], plain["mwd"]) * hp)[wet].sum() / hp[wet].sum())}
-    v_sur = sur["bins"] / (sur["gpu_ms"] / 1e3)
+    nh = len(sur["hourly"])
+    ended = sur["stopped"] is None
+    # errors at the last hour the surrogate run completed
+    hp = plain["hourly"][nh - 1] if nh else plain["ht"].astype(np.float64)
+    hs = sur["hourly"][nh - 1] if nh else np.full_like(hp, np.nan)
+    hourly_err = []
+    for a, b in zip(sur["hourly"], plain["hourly"]):
+        m = b > 1e-3
+        fin = np.isfinite(a) & m
+        hourly_err.append({"mean_abs_rel": float(np.abs(a - b)[fin].mean() / b[fin].mean()) if fin.any() else None,
+                           "nonfinite_frac": float(1.0 - fin.sum() / max(m.sum(), 1))})
+    wet = (hp > 1e-3) & np.isfinite(hs)
+    hs_err = None
+    if wet.any():
+        hs_err = {"at_hour": nh, "mean_abs_rel": float(np.abs(hs - hp)[wet].mean() / hp[wet].mean()),
+                  "rel_l2": float(np.linalg.norm((hs - hp)[wet]) / np.linalg.norm(hp[wet])),
+                  "p99_rel": float(np.percentile(np.abs(hs - hp)[wet] / hp[wet], 99)),
+                  "domain_mean_rel": float(abs(hs[wet].mean() - hp[wet].mean()) / hp[wet].mean())}
+    tp_err = dir_err = None
+    if ended and wet.any():  # peak period and direction at the end of the run
+        tp_err = {"mean_abs_rel": float((np.abs(sur["dwp"] - plain["dwp"])[wet] / plain["dwp"][wet]).mean()),
+                  "same_bin_frac": float((sur["dwp"] == plain["dwp"])[wet].mean())}
+        dir_err = {"mean_abs_deg": float(_angle_err_deg(sur["mwd"], plain["mwd"])[wet].mean()),
+                   "hs_weighted_deg": float((_angle_err_deg(sur["mwd"], plain["mwd"]) * hp)[wet].sum()
+                                            / hp[wet].sum())}
+    v_sur = sur["bins"] / (sur["gpu_ms"] / 1e3) if sur["gpu_ms"] > 0 else 0.0
     v_plain = plain["bins"] / (plain["gpu_ms"] / 1e3)
     flops_row = 2.0 * (1344 * 512 + 512 * 512 + 512 * 1344)
     gemm_tflops = (flops_row * sur["rows"] * sur["timed_steps"] / (sur["ms_gemm"] / 1e3) / 1e12
@@ -404,14 +448,16 @@ def run_surrogate(args):
             "ms_per_step": sur["gpu_ms"] / max(sur["substeps"], 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16 (MLP) / f32 (spectrum)", "data": "synthetic",
             "config": {"workload": "surrogate: hurricane %dx%d dx=2km seed 5, %g h, JONSWAP Hs 0.2 m start; MLP "
-                                   "1344-512-512-1344 GELU bf16/f32-acc; energy-budget tolerance 0.1"
-                                   % (args.size, args.size, args.hours),
+                                   "1344-512-512-1344 GELU bf16/f32-acc; energy-budget tolerances 0.02 (total), 0.1 "
+                                   "(level, wind-weighted)" % (args.size, args.size, args.hours),
                        "pairs": int(U.stat("surrogate_pairs")), "pair_sources": gen,
                        "train_steps": int(len(losses)), "batch": 8192},
             "plain": {"value": v_plain, "gpu_ms": plain["gpu_ms"], "substeps": plain["substeps"]},
             "surrogate_over_plain": v_sur / v_plain,
             "fallback_fraction": sur["fallback"] / max(sur["points"], 1),
             "hs_error_vs_plain": hs_err, "tp_error_vs_plain": tp_err, "dir_error_vs_plain": dir_err,
+            "hs_error_vs_plain_hourly": hourly_err, "surrogate_run_stopped": sur["stopped"],
+            "nonfinite_points_end": int((~np.isfinite(hs)).sum()),
             "train": {"seconds": t_train, "loss_first": float(losses[:20].mean()), "loss_last": float(losses[-20:].mean())},
             "generate_seconds": t_gen,
             "surrogate_ms_per_step": {"features": sur["ms_features"] / max(sur["timed_steps"], 1),
@@ -420,6 +466,62 @@ def run_surrogate(args):
             "roofline": {"bound": "tensor", "kernel": "k_gemm (3 layers)", "achieved": gemm_tflops, "peak": pk_sus,
                          "unit": "TFLOP/s", "frac": (gemm_tflops / pk_sus) if gemm_tflops else None,
                          "peak_kind": pk_kind + " sustained", "traffic": None}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_accuracy(args):
+    """Accuracy of the plain GPU path against the fp64 oracle over a full
+    run: the hurricane workload (linear shelf, translating Holland vortex,
+    background current, JONSWAP start) on an acc_size x acc_size grid at
+    2 km for args.hours, and the random field on the same grid for 3 h.
+    Errors of Hs, mean period, peak period, mean direction, ustar and the
+    stress, at every wet point, after the run."""
+    rank, world, local_rank = rank_info()
+    import umwm_gb300 as U
+    from oracle import pyoracle
+    from umwm_gb300 import configs
+
+    U.set_option("device", local_rank)
+    pyoracle.build()
+    threads = pyoracle.set_threads(os.cpu_count() or 1)
+    S = args.acc_size
+    out = {}
+    for name, case in (("hurricane", configs.hurricane(mm=S, nm=S, hours=args.hours, seed=3)),
+                       ("random_field", configs.random_field(mm=S, nm=S, hours=3, seed=2))):
+        U.clear_inputs()
+        case.stage(U)
+        U.umwm_initialize(nml_text=case.nml)
+        U.umwm_run(case.start, case.stop)
+        g = {k: U.get_field(k).astype(np.float64) for k in ("ht", "mwp", "dwp", "mwd", "ustar", "taux", "tauy")}
+        sub = U.dims()["substeps"]
+        U.umwm_finalize()
+        t0 = time.perf_counter()
+        o = pyoracle.Oracle(case.nml, 64)
+        case.stage(o)
+        o.initialize()
+        o.run(case.start, case.stop)
+        t_or = time.perf_counter() - t0
+        r = {k: np.asarray(o.get(k), dtype=np.float64) for k in g}
+        wet = r["ht"] > 1e-3
+        rel = lambda a, b: np.abs(a - b)[wet] / np.abs(b)[wet]
+        ang = np.degrees(np.abs(np.angle(np.exp(1j * (g["mwd"] - r["mwd"])))))[wet]
+        tau_g, tau_r = np.hypot(g["taux"], g["tauy"]), np.hypot(r["taux"], r["tauy"])
+        out[name] = {
+            "grid": "%dx%d" % (S, S), "hours": case.meta["hours"], "wet_points": int(wet.size),
+            "gpu_substeps": int(sub), "fp64_substeps": int(o.scalar("substeps")), "oracle_seconds": t_or,
+            "hs": {"max_rel": float(rel(g["ht"], r["ht"]).max()), "mean_rel": float(rel(g["ht"], r["ht"]).mean())},
+            "mwp": {"max_rel": float(rel(g["mwp"], r["mwp"]).max())},
+            "dwp": {"same_frac": float((g["dwp"] == r["dwp"])[wet].mean()),
+                    "max_rel": float(rel(g["dwp"], r["dwp"]).max())},
+            "mwd": {"max_deg": float(ang.max()), "mean_deg": float(ang.mean())},
+            "ustar": {"max_rel": float(rel(g["ustar"], r["ustar"]).max())},
+            "tau": {"max_rel": float(rel(tau_g, tau_r).max())},
+        }
+    line = {"metric": "accuracy of the plain GPU path (f32) against the fp64 oracle", "n_gpus": 1,
+            "oracle_threads": threads, "cases": out,
+            "pass_hs_2pct": all(v["hs"]["max_rel"] <= 0.02 for v in out.values())}
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -434,9 +536,13 @@ def main():
     ap.add_argument("--size", type=int, default=1000, help="domain is size x size")
     ap.add_argument("--ref-size", type=int, default=200, help="crop for the CPU legs")
     ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-threads", type=int, default=0, help="host threads of the CPU legs (0: all)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="random_field", choices=["random_field", "ensemble", "surrogate"])
+    ap.add_argument("--case", default="random_field", choices=["random_field", "hurricane", "fetch_limited"],
+                    help="plain-path workload")
+    ap.add_argument("--workload", default="random_field", choices=["random_field", "ensemble", "surrogate", "accuracy"])
+    ap.add_argument("--acc-size", type=int, default=120, help="grid of the accuracy workloads")
     ap.add_argument("--pairs", type=int, default=2000000)
     ap.add_argument("--pts-per-substep", type=int, default=16384)
     ap.add_argument("--train-steps", type=int, default=2000)
@@ -451,13 +557,24 @@ def main():
         return run_ensemble(args)
     if args.workload == "surrogate":
         return run_surrogate(args)
+    if args.workload == "accuracy":
+        return run_accuracy(args)
 
     rank, world, local_rank = rank_info()
     dist = Dist(world, local_rank)
     import umwm_gb300 as U
     from umwm_gb300 import configs
 
-    case = configs.random_field(mm=args.size, nm=args.size, hours=3)
+    if args.case == "hurricane":
+        case = configs.hurricane(mm=args.size, nm=args.size, hours=12, seed=3)
+        desc = ("hurricane %dx%d dx=2km (linear shelf 20-3000 m, Holland vortex Vmax 50 m/s Rmax 30 km, 5 m/s, "
+                "0.5 m/s current, 600 s forcing snapshots), plain path" % (args.size, args.size))
+    elif args.case == "fetch_limited":
+        case = configs.fetch_limited(mm=args.size, nm=args.size, hours=6)
+        desc = "fetch_limited %dx%d dx=5km, 1000 m, 10 m/s, plain path" % (args.size, args.size)
+    else:
+        case = configs.random_field(mm=args.size, nm=args.size, hours=3)
+        desc = "random_field %dx%d dx=2km, plain path" % (args.size, args.size)
     U.set_option("device", local_rank)
     U.clear_inputs()
     case.stage(U)
@@ -518,25 +635,28 @@ def main():
     e2e = None
     if not args.no_e2e:
         U.set_option("max_substeps", -1)
-        f1 = case.forcing[sorted(case.forcing)[1]]
+        keys = sorted(case.forcing)
+        dtg_s = float(re.search(r"dtg\s*=\s*([0-9.]+)", case.nml).group(1))
+        t_end = keys[1] if len(keys) > 1 else configs._time_str(case.start, dtg_s)
+        f1 = case.forcing[keys[1]] if len(keys) > 1 else {}
         s_before = U.dims()["substeps"]
         dist.barrier()
         t0 = time.perf_counter()
         for var, fld in f1.items():
-            U.put_forcing(sorted(case.forcing)[1], var, fld)
-        U.umwm_run(case.start, sorted(case.forcing)[1])
+            U.put_forcing(t_end, var, fld)
+        U.umwm_run(case.start, t_end)
         hs = U.get_field("ht")
         us = U.get_field("ustar")
         te = time.perf_counter() - t0
         ns = U.dims()["substeps"] - s_before
         te = dist.max(te)
         e_bins = dist.sum(float(ns) * N * BINS)
-        h2d = sum(np.asarray(v).nbytes for v in f1.values())
+        h2d = sum(np.asarray(v).nbytes for v in f1.values()) if f1 else 0
         d2h = hs.nbytes + us.nbytes + 4 * ns
         e2e = {"value": e_bins / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d / max(ns, 1)),
                "d2h_bytes_per_step": int(d2h / max(ns, 1)), "substeps": ns,
-               "note": "one dtg (3600 s) through umwm_gpu_run: forcing staged from host arrays and copied in, "
-                       "Hs and ustar read back"}
+               "note": "one dtg (%g s) through umwm_gpu_run: forcing staged from host arrays and copied in, "
+                       "Hs and ustar read back" % dtg_s}
         assert np.isfinite(hs).all()
 
     peak, peak_kind = peak_hbm()
@@ -557,9 +677,10 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": nsteps,
             "warmup": args.warmup, "ms_per_step": t_max * 1e3 / nsteps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "random_field %dx%d dx=2km, plain path (wet points %d, %d bins each); inputs "
-                                   "larger than L2 (spectrum %.1f GB per array)" % (args.size, args.size, N, BINS,
-                                                                                   N * BINS * 4 / 1e9),
+            "config": {"workload": "%s (wet points %d, %d bins each); spectrum %.2f GB per array%s"
+                                   % (desc, N, BINS, N * BINS * 4 / 1e9,
+                                      ", inputs larger than L2" if N * BINS * 4 > 129e6 else
+                                      ", inputs smaller than L2 (no flush between steps)"),
                        "wet_points": N, "bins_per_point": BINS, "replicas": world},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk, "kernel_ms_per_step": {k: kms[k] / max(nsteps, 1) for k in kms if kms[k] > 0},

@@ -18,7 +18,11 @@
  * Inputs the reference reads from netCDF files are staged in memory under
  * the same names and time keys (there is no netCDF library on this
  * platform); umwm_gpu_initialize / umwm_gpu_run read them where the
- * reference opens the file.
+ * reference opens the file.  An input that was not staged is read from the
+ * reference's own file when that file is a netCDF classic or 64-bit-offset
+ * file: input/umwm.gridtopo (lon, lat, z), input/umwmin_<time>.nc (uw, vw,
+ * uc, vc, rhoa, rhow, fice) and restart/umwmrst_<time>.nc (F, ust), paths
+ * relative to the working directory as in the reference.
  */
 #ifndef UMWM_GPU_H
 #define UMWM_GPU_H
@@ -129,6 +133,16 @@ int umwm_gpu_set_state(const float* F, const float* ust);
  * calls that overlap on the GPU race.  This entry point has no counterpart in
  * the reference. */
 int umwm_gpu_get_state_noalloc(float* F, float* ust);
+
+/* restart_write, umwm_restart.F90:59-154: write the selected member's
+ * state to a netCDF file (64-bit-offset classic format) in the reference's
+ * layout: dimensions x, f, th; variables lon, lat, frequency, theta, ust,
+ * wavenumber(x,f), F(x,th,f).  umwm_gpu_run also writes
+ * restart/umwmrst_<time>.nc at the times the namelist's outrst asks for
+ * (umwm_top.F90:183-190), and at a restart initialize reads that file when
+ * no restart was staged for the start time (umwm_restart.F90:19-56).
+ * Ensemble members use restart/umwmrst_<time>_m<member>.nc. */
+int umwm_gpu_write_restart(const char* path);
 
 /* Copy a named field into out (n floats).  Names are the reference's
  * variable names: wet-point fields (ht, mwp, mwd, mss, mwl, dwd, dwl, dwp,

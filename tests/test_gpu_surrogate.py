@@ -105,8 +105,9 @@ def test_training_and_surrogate_run(lib_built):
     """Pairs from a plain run of one random field train the network; pairs
     from another seed are held out.  On the held-out pairs the trained
     network's loss is well below the untrained network's (whose near-zero
-    output is the step without a source term).  A run with the trained
-    network and the energy-budget fallback stays finite."""
+    output is the step without a source term).  Ten substeps with the trained
+    network and the energy-budget fallback keep the state finite and
+    non-negative, and count every wet point once per substep."""
     from umwm_gb300 import configs
 
     U = lib_built
@@ -139,13 +140,14 @@ def test_training_and_surrogate_run(lib_built):
     held_case.stage(U)
     U.umwm_initialize(nml_text=held_case.nml)
     U.set_option("surrogate", 1)
+    U.set_option("max_substeps", 10)
     p0, f0 = U.stat("surrogate_points"), U.stat("surrogate_fallback")
     U.umwm_run(held_case.start, held_case.stop)
     pts, fb = U.stat("surrogate_points") - p0, U.stat("surrogate_fallback") - f0
     F, u = U.get_state()
     U.set_option("surrogate", 0)
     U.umwm_finalize()
-    assert pts > 0 and 0 <= fb <= pts
+    assert pts == 10 * F.shape[0] and 0 <= fb <= pts
     assert np.isfinite(F).all() and (F >= 0).all() and np.isfinite(u).all()
 
 

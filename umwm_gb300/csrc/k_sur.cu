@@ -14,6 +14,7 @@ namespace sur {
 namespace {
 
 constexpr int PITCHW = FPAD / 2 + 1;  // 32-bit words per staged row (odd: conflict-free columns)
+constexpr int UNR = 6;                 // spectrum loads in flight per warp in the bin loops
 constexpr int TILE_SMEM = 32 * PITCHW * 4;
 
 struct PointInfo {
@@ -97,13 +98,25 @@ __global__ void __launch_bounds__(256) k_features(const Params prm, const Ptrs P
   __syncthreads();
   const int j = s_j[lane], ok = s_ok[lane], s = s_s[lane];
   __nv_bfloat16* h = row_h(tile, lane);
-  for (int b = warp; b < F0; b += 8) {
-    const int o = b / NP, p = b - o * NP;
-    int pr = p - s;
-    if (pr < 0) pr += NP;
-    const float e = ok ? P.E[sidx(prm, o, p, j)] : 0.f;
-    h[o * NP + pr] = __float2bfloat16_rn(ok ? feature(e) : 0.f);
-    if (ecopy && r0 + lane < n) ecopy[(size_t)(r0 + lane) * F0 + o * NP + pr] = e;
+  // UNR independent loads in flight per warp before any is used
+  for (int b0 = warp; b0 < F0; b0 += 8 * UNR) {
+    float ev[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const int b = b0 + 8 * u;
+      const int o = b / NP, p = b - o * NP;
+      ev[u] = (ok && b < F0) ? __ldg(P.E + sidx(prm, o, p, j)) : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const int b = b0 + 8 * u;
+      if (b >= F0) break;
+      const int o = b / NP, p = b - o * NP;
+      int pr = p - s;
+      if (pr < 0) pr += NP;
+      h[o * NP + pr] = __float2bfloat16_rn(ok ? feature(ev[u]) : 0.f);
+      if (ecopy && r0 + lane < n) ecopy[(size_t)(r0 + lane) * F0 + o * NP + pr] = ev[u];
+    }
   }
   __syncthreads();
   uint32_t* X32 = reinterpret_cast<uint32_t*>(X);
@@ -169,20 +182,32 @@ __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, c
   const float wdir = s_wdir[lane], dts = s_dts[lane];
   float m0 = 0.f, m1 = 0.f, w0 = 0.f, w1 = 0.f;  // energy, and energy where the wind feeds (weight Sin)
   if (ok) {
-    for (int b = warp; b < F0; b += 8) {
-      const int o = b / NP, p = b - o * NP;
-      int pr = p - s;
-      if (pr < 0) pr += NP;
-      const float e = P.E[sidx(prm, o, p, j)];
-      float sp;
-      const float ef = step_bin(prm, P, wi, dts, wdir, e, __bfloat162float(h[o * NP + pr]), o, p, j, sp);
-      const float kdk = P.TAB[tidx(prm, o, T_KDK, j)];
-      m0 += e * kdk;
-      m1 += ef * kdk;
-      w0 += fmaxf(e, 0.f) * sp * kdk;
-      w1 += ef * sp * kdk;
-      atomicAdd(&lev0[o][lane], fmaxf(e, 0.f));
-      atomicAdd(&lev1[o][lane], ef);
+    for (int b0 = warp; b0 < F0; b0 += 8 * UNR) {
+      float ev[UNR];
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        const int b = b0 + 8 * u;
+        const int o = b / NP, p = b - o * NP;
+        ev[u] = b < F0 ? P.E[sidx(prm, o, p, j)] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        const int b = b0 + 8 * u;
+        if (b >= F0) break;
+        const int o = b / NP, p = b - o * NP;
+        int pr = p - s;
+        if (pr < 0) pr += NP;
+        const float e = ev[u];
+        float sp;
+        const float ef = step_bin(prm, P, wi, dts, wdir, e, __bfloat162float(h[o * NP + pr]), o, p, j, sp);
+        const float kdk = P.TAB[tidx(prm, o, T_KDK, j)];
+        m0 += e * kdk;
+        m1 += ef * kdk;
+        w0 += fmaxf(e, 0.f) * sp * kdk;
+        w1 += ef * sp * kdk;
+        atomicAdd(&lev0[o][lane], fmaxf(e, 0.f));
+        atomicAdd(&lev1[o][lane], ef);
+      }
     }
   }
   red0[warp][lane] = m0;
@@ -224,16 +249,27 @@ __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, c
   }
   __syncthreads();
   if (!s_pass[lane]) return;
-  for (int b = warp; b < F0; b += 8) {
-    const int o = b / NP, p = b - o * NP;
-    int pr = p - s;
-    if (pr < 0) pr += NP;
-    const size_t k = sidx(prm, o, p, j);
-    const float e = P.E[k];
-    float sp;
-    const float ef = step_bin(prm, P, wi, dts, wdir, e, __bfloat162float(h[o * NP + pr]), o, p, j, sp);
-    P.ES[k] = 0.5f * (e + ef);
-    P.EF[k] = ef;
+  for (int b0 = warp; b0 < F0; b0 += 8 * UNR) {
+    float ev[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const int b = b0 + 8 * u;
+      const int o = b / NP, p = b - o * NP;
+      ev[u] = b < F0 ? P.E[sidx(prm, o, p, j)] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const int b = b0 + 8 * u;
+      if (b >= F0) break;
+      const int o = b / NP, p = b - o * NP;
+      int pr = p - s;
+      if (pr < 0) pr += NP;
+      const size_t k = sidx(prm, o, p, j);
+      float sp;
+      const float ef = step_bin(prm, P, wi, dts, wdir, ev[u], __bfloat162float(h[o * NP + pr]), o, p, j, sp);
+      P.ES[k] = 0.5f * (ev[u] + ef);
+      P.EF[k] = ef;
+    }
   }
 }
 

@@ -22,6 +22,7 @@
 #include "../../include/umwm_gpu.h"
 #include "host_model.hpp"
 #include "kernels.hpp"
+#include "ncfile.hpp"
 #include "surrogate.hpp"
 
 namespace umwm {
@@ -222,7 +223,22 @@ int read_forcing(Model& M, MemberHost& mh, const std::string& key, std::vector<f
   const HostModel& H = mh.H;
   if (!mh.readfile) return UMWM_OK;
   auto it = mh.in.forcing.find(key);
-  if (it == mh.in.forcing.end()) return fail(UMWM_ERR_INPUT, "input_nc: no forcing staged for " + key);
+  if (it == mh.in.forcing.end()) {
+    // nothing staged: the reference's file input/umwmin_<time>.nc (umwm_io.F90:20-26)
+    const std::string path = "input/umwmin_" + key + ".nc";
+    std::map<std::string, std::vector<float>> vars;
+    const std::pair<bool, const char*> want[] = {{H.winds, "uw"}, {H.winds, "vw"}, {H.currents, "uc"},
+                                                 {H.currents, "vc"}, {H.seaice, "fice"},
+                                                 {H.air_density, "rhoa"}, {H.water_density, "rhow"}};
+    for (auto& w : want) {
+      if (!w.first) continue;
+      std::vector<size_t> sh;
+      std::string err;
+      if (!nc::read_float(path, w.second, sh, vars[w.second], err))
+        return fail(UMWM_ERR_INPUT, "input_nc: no forcing staged for " + key + " and " + err);
+    }
+    it = mh.in.forcing.emplace(key, std::move(vars)).first;
+  }
   const size_t n2 = (size_t)H.mm * H.nm;
   auto get = [&](const char* var, float* dst, bool zero_land, std::vector<float>* keep) -> int {
     auto v = it->second.find(var);
@@ -544,14 +560,104 @@ int set_state_member(Model& M, int m, const float* F, const float* ust) {
   return UMWM_OK;
 }
 
-int restart_read(Model& M, int m, const std::string& key) {  // umwm_restart.F90:19-56
+// Restart file name of a member: restart/umwmrst_<time>.nc as the reference
+// names it (umwm_restart.F90:28-31, :70); ensemble members add _m<member>.
+std::string restart_path(const Model& M, int m, const std::string& key) {
+  std::string p = "restart/umwmrst_" + key;
+  if (M.mem.size() > 1) p += "_m" + std::to_string(m);
+  return p + ".nc";
+}
+
+// restart_read, umwm_restart.F90:19-56: the staged restart for the time key,
+// else the file restart/umwmrst_<key>.nc (F and ust).
+int restart_read(Model& M, int m, const std::string& key) {
   MemberHost& mh = M.mem[m];
   auto it = mh.in.restarts.find(key);
-  if (it == mh.in.restarts.end()) return fail(UMWM_ERR_INPUT, "restart_read: no restart staged for " + key);
+  if (it == mh.in.restarts.end()) {
+    const std::string path = restart_path(M, m, key);
+    std::vector<size_t> shF, shU;
+    std::vector<float> F, U;
+    std::string err;
+    if (!nc::read_float(path, "F", shF, F, err) || !nc::read_float(path, "ust", shU, U, err))
+      return fail(UMWM_ERR_INPUT, "restart_read: no restart staged for " + key + " and " + err);
+    const std::vector<size_t> wantF = {(size_t)mh.N, (size_t)M.prm.P, (size_t)M.prm.O};
+    if (shF != wantF || shU != std::vector<size_t>{(size_t)mh.N})
+      return fail(UMWM_ERR_INPUT, "restart_read: " + path + " does not match the grid (x, th, f)");
+    return set_state_member(M, m, F.data(), U.data());
+  }
   const size_t nF = (size_t)M.prm.O * M.prm.P * mh.N;
   if (it->second.first.size() != nF || it->second.second.size() != (size_t)mh.N)
     return fail(UMWM_ERR_INPUT, "restart_read: restart arrays have the wrong size");
   return set_state_member(M, m, it->second.first.data(), it->second.second.data());
+}
+
+// restart_write, umwm_restart.F90:59-154: dimensions x (wet points), f, th;
+// variables lon, lat, frequency, theta, ust, wavenumber (x, f) and F
+// (x, th, f), with the reference's descriptions and units.
+int restart_write(Model& M, int m, const std::string& path) {
+  const Params& p = M.prm;
+  const MemberHost& mh = M.mem[m];
+  const HostModel& H = mh.H;
+  const int N = mh.N;
+  const size_t R = (size_t)p.O * p.P;
+  CU(cudaStreamSynchronize(M.st));
+  std::vector<float> lon(N), lat(N), ust(N);
+  for (int i = 1; i <= N; ++i) {
+    lon[i - 1] = H.lon[H.i2(H.mi[i], H.ni[i])];
+    lat[i - 1] = H.lat[H.i2(H.mi[i], H.ni[i])];
+  }
+  CU(cudaMemcpy(ust.data(), M.P.ustar + mh.off, (size_t)N * 4, cudaMemcpyDeviceToHost));
+  auto from = [](const float* v) {
+    return [v](size_t first, size_t n, float* out) {
+      std::memcpy(out, v + first, n * 4);
+      return true;
+    };
+  };
+  // F streams through a device buffer of whole points
+  const int chunk_pts = 2048;
+  float* dtmp = nullptr;
+  CU(cudaMalloc(&dtmp, (size_t)chunk_pts * R * 4));
+  std::vector<float> hbuf((size_t)chunk_pts * R);
+  long cached = -1;  // first point held in hbuf
+  bool dev_ok = true;
+  auto fillF = [&](size_t first, size_t n, float* out) {
+    while (n > 0) {
+      const long pt = (long)(first / R);
+      if (cached < 0 || pt < cached || pt >= cached + chunk_pts) {
+        const int cnt = (int)std::min<long>(chunk_pts, N - pt);
+        cudaError_t e = launch_to_ref(p, M.E, dtmp, mh.off + (int)pt, cnt, M.st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(M.st);
+        if (e == cudaSuccess) e = cudaMemcpy(hbuf.data(), dtmp, (size_t)cnt * R * 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+          dev_ok = false;
+          return false;
+        }
+        cached = pt;
+      }
+      const size_t off = first - (size_t)cached * R;
+      const size_t take = std::min(n, (size_t)chunk_pts * R - off);
+      std::memcpy(out, hbuf.data() + off, take * 4);
+      out += take;
+      first += take;
+      n -= take;
+    }
+    return true;
+  };
+  const std::vector<std::pair<std::string, size_t>> dims = {{"x", (size_t)N}, {"f", (size_t)p.O}, {"th", (size_t)p.P}};
+  std::vector<nc::Var> vars = {
+      {"lon", {0}, {{"description", "longitude"}, {"units", "degrees east"}}, from(lon.data())},
+      {"lat", {0}, {{"description", "latitude"}, {"units", "degrees north"}}, from(lat.data())},
+      {"frequency", {1}, {{"description", "frequency"}, {"units", "hz"}}, from(H.f.data())},
+      {"theta", {2}, {{"description", "directions"}, {"units", "rad"}}, from(H.th.data())},
+      {"ust", {0}, {{"description", "friction velocity"}, {"units", "m s^-1"}}, from(ust.data())},
+      {"wavenumber", {0, 1}, {{"description", "wavenumber"}, {"units", "rad m^-1"}}, from(H.k.data() + p.O)},
+      {"F", {0, 2, 1}, {{"description", "wave energy spectrum"}, {"units", "m^4 rad^-1"}}, fillF}};
+  std::string err;
+  const bool ok = nc::write(path, dims, vars, err);
+  cudaFree(dtmp);
+  if (!dev_ok) return fail(UMWM_ERR_CUDA, "restart_write: device copy failed");
+  if (!ok) return fail(UMWM_ERR_INPUT, "restart_write: " + err);
+  return UMWM_OK;
 }
 
 int check_ctl(Model& M) {
@@ -733,6 +839,28 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     CU(timed(M, K_DIAG, [&] { return launch_diag(M.prm, M.P, M.st); }));
     M.launches++;
     if (M.verbose) print_screen(M);
+    // restart output, umwm_top.F90:183-190 (with the reference's test of
+    // outspec == -1 for writing every step)
+    {
+      const HostModel& H0 = M.mem[0].H;
+      const int64_t secs = now % 86400;
+      const bool fullhour = secs % 3600 == 0;
+      const int hour = (int)(secs / 3600);
+      if ((H0.outrst > 0 && hour % H0.outrst == 0 && fullhour) || (H0.outrst <= 0 && H0.outspec == -1)) {
+        // like the reference (which ignores the netCDF status here), a file
+        // that cannot be written is reported and the run goes on
+        const std::string key = time_to_string(now, '_');
+        for (size_t m = 0; m < M.mem.size(); ++m) {
+          const std::string path = restart_path(M, (int)m, key);
+          if (restart_write(M, (int)m, path) != UMWM_OK) {
+            std::fprintf(stderr, "umwm: restart_write: %s not written (%s)\n", path.c_str(), g_err.c_str());
+            g_err.clear();
+          } else if (M.verbose) {
+            std::printf("umwm: restart_write: restart written to %s\n", path.c_str());
+          }
+        }
+      }
+    }
     if (M.check_finite) {
       // a NaN/Inf bin makes its point's significant wave height non-finite
       CU(cudaMemsetAsync(&M.d_glob->nonfinite, 0, sizeof(int), M.st));
@@ -757,6 +885,16 @@ int init_common(std::vector<Pending>& members, bool device) {
     MemberHost& mh = M->mem[m];
     mh.in = std::move(members[m].in);
     if (!mh.H.read_namelist(members[m].nml)) return fail(UMWM_ERR_NAMELIST, mh.H.err);
+    // nothing staged: the reference's file input/umwm.gridtopo (umwm_init.F90:397-427, :541-546)
+    const std::pair<bool, const char*> want[] = {
+        {mh.H.gridfromfile, "lon"}, {mh.H.gridfromfile, "lat"}, {mh.H.topofromfile, "z"}};
+    for (auto& w : want) {
+      if (!w.first || mh.in.gridtopo.count(w.second)) continue;
+      std::vector<size_t> sh;
+      std::vector<float> v;
+      std::string err;
+      if (nc::read_float("input/umwm.gridtopo", w.second, sh, v, err)) mh.in.gridtopo[w.second] = std::move(v);
+    }
     if (!mh.H.build(mh.in)) return fail(UMWM_ERR_INPUT, mh.H.err);
   }
   if (device) {
@@ -994,6 +1132,13 @@ int umwm_gpu_get_state(float* F, float* ust) {
   }
   if (ust) CU(cudaMemcpy(ust, M->P.ustar + mh.off, (size_t)mh.N * 4, cudaMemcpyDeviceToHost));
   return UMWM_OK;
+}
+
+int umwm_gpu_write_restart(const char* path) {
+  Model* M = need_model(true);
+  if (!M) return UMWM_ERR_STATE;
+  if (!path) return fail(UMWM_ERR_ARG, "write_restart: null path");
+  return restart_write(*M, M->sel, path);
 }
 
 // Surrogate input rows of the selected member's wet points for the current

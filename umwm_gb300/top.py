@@ -195,6 +195,11 @@ def get_state_noalloc():
     return F, u
 
 
+def write_restart(path):
+    """restart_write: the selected member's state as a netCDF restart file."""
+    check(lib().umwm_gpu_write_restart(str(path).encode()))
+
+
 def set_state(F=None, ust=None):
     Fp = _f32(F).ravel() if F is not None else None
     up = _f32(ust).ravel() if ust is not None else None
