@@ -133,9 +133,11 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : 3) k_advect(const Params prm
   float sx = 0.f, sy = 0.f, dsx = 0.f, dsy = 0.f, txom = 0.f, tyom = 0.f;
   // E* and ef of this block two frequencies ahead go to L2 in the background
   const size_t blk = sidx(prm, 0, 0, jj & ~31);
+  // E* is read only at propagated levels o < oc (the warp's largest oc bounds them)
+  const int ocw = (int)__reduce_max_sync(0xffffffffu, (unsigned)max(oc, 0));
   auto pf = [&](int o) {
     if (o < O && lane == 0) {
-      bulk_prefetch(P.ES + blk + (size_t)o * lstride, (unsigned)(prm.P * 128));
+      if (o < ocw) bulk_prefetch(P.ES + blk + (size_t)o * lstride, (unsigned)(prm.P * 128));
       bulk_prefetch(P.EF + blk + (size_t)o * lstride, (unsigned)(prm.P * 128));
     }
   };
@@ -225,7 +227,8 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : 3) k_advect(const Params prm
       // (e k^4)^sds_power NaN); round-off negatives after a surrogate step
       // are cut to 0 here, which leaves every plain-path result unchanged
       ef[k] = ef[k] < 0.f ? 0.f : ef[k];  // NaN stays NaN (the finite check must see it)
-      if (valid) Eo[oS + k * 32] = ef[k];
+      // above the cut-off e = ef is already in place (EF aliases E)
+      if (valid && prog) Eo[oS + k * 32] = ef[k];
       const float s = sin_dir(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], cp0, fkovg, tail);
       const float es_ = ef[k] * s;
       tx += es_ * prm.cth[k];

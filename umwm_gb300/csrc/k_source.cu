@@ -151,8 +151,11 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? 3 : 4
   const float* Eb = P.E + sidx(prm, 0, q * H, jj);
   const float* Tb = P.TAB + tidx(prm, 0, 0, jj);
   const float* Eblk = P.E + sidx(prm, 0, 0, jj & ~31);  // start of this block's region
+  // the dts pre-pass needs only the prognostic levels o < oc (the mss prefix
+  // of a level uses the levels below it): the warp stops at its largest oc
+  const int OP = INTEG ? O : min(O, (int)__reduce_max_sync(0xffffffffu, (unsigned)max(wi.oc, 0)));
   auto pf = [&](int o) {
-    if (o < O && lane == 0 && (G == 2 || (w * PW) % 32 == 0))
+    if (o < OP && lane == 0 && (G == 2 || (w * PW) % 32 == 0))
       bulk_prefetch_l2(Eblk + (size_t)o * lstride, (unsigned)(prm.P * 128));
   };
   pf(0);
@@ -166,7 +169,7 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? 3 : 4
   for (int k = 0; k < H; ++k) { ec[k] = sc[k] = e1[k] = s1[k] = e2[k] = s2[k] = 0.f; }
   Coef Cc{}, C1{}, C2{};
 
-  const int OL = INTEG ? O + 2 : O;
+  const int OL = INTEG ? O + 2 : OP;
   for (int o = 0; o < OL; ++o) {
     pf(o + 2);
     if (o < O) {
