@@ -1343,9 +1343,15 @@ struct Model {
         sin_d12(); sds_d12(); snl_d12(); s_ice(); source();
         propagation();
         refraction();
+        // e = ef (umwm_top.F90:113), with negatives cut to 0 as the GPU path
+        // does: the explicit Snl term can leave a tiny negative ef, after
+        // which (e k^4)^sds_power is NaN (seen in fp64 on the hurricane case)
         for (int q = istart; q <= iend; ++q)
           for (int p = 1; p <= pm; ++p)
-            for (int o = 1; o <= om; ++o) e[opi(o, p, q)] = ef[opi(o, p, q)];
+            for (int o = 1; o <= om; ++o) {
+              const T v = ef[opi(o, p, q)];
+              e[opi(o, p, q)] = v < T(0) ? T(0) : v;
+            }
         stress_atm();
         if (first) { diag(); first = false; }
         substeps++;

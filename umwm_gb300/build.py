@@ -41,6 +41,17 @@ def _stale(obj, deps):
 def build(verbose=False, extra_nvcc=()):
     os.makedirs(OUT_DIR, exist_ok=True)
     os.makedirs(BUILD_DIR, exist_ok=True)
+    # extra nvcc definitions for tuning experiments (e.g. "-DUMWM_INTEG_MINB=4");
+    # a change of flags rebuilds everything
+    extra_nvcc = list(extra_nvcc) + os.environ.get("UMWM_NVCC_DEFS", "").split()
+    stamp = os.path.join(BUILD_DIR, "flags.txt")
+    flags = " ".join(NVCC_FLAGS + extra_nvcc)
+    if not os.path.exists(stamp) or open(stamp).read() != flags:
+        for f in os.listdir(BUILD_DIR):
+            if f.endswith(".o"):
+                os.remove(os.path.join(BUILD_DIR, f))
+        with open(stamp, "w") as fh:
+            fh.write(flags)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".hpp", ".h"))]
     headers.append(os.path.join(os.path.dirname(HERE), "include", "umwm_gpu.h"))
     jobs, objs = [], []

@@ -54,8 +54,12 @@ __device__ __forceinline__ float sin_dir(const Params& prm, const WindIn& w, flo
   return s;
 }
 
+#ifndef UMWM_ADVECT_MINB
+#define UMWM_ADVECT_MINB 3  // resident CTAs per SM the register budget is sized for (two groups)
+#endif
+
 template <int G, int H, bool CURV>
-__global__ void __launch_bounds__(128, G == 4 ? 4 : 3) k_advect(const Params prm, const Ptrs P) {
+__global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(const Params prm, const Ptrs P) {
   constexpr int PW = 32 / G;   // points per warp
   constexpr int PPC = 4 * PW;  // points per CTA (4 warps)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -223,9 +227,9 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : 3) k_advect(const Params prm
     float tx = 0.f, ty = 0.f;
 #pragma unroll
     for (int k = 0; k < H; ++k) {
-      // e >= 0 after every plain step (a negative e would make the reference's
-      // (e k^4)^sds_power NaN); round-off negatives after a surrogate step
-      // are cut to 0 here, which leaves every plain-path result unchanged
+      // negatives are cut to 0: the explicit Snl term (snl_d12) can leave a
+      // tiny negative ef, and a negative e makes the next step's
+      // (e k^4)^sds_power NaN (the oracle cuts them at the same point)
       ef[k] = ef[k] < 0.f ? 0.f : ef[k];  // NaN stays NaN (the finite check must see it)
       // above the cut-off e = ef is already in place (EF aliases E)
       if (valid && prog) Eo[oS + k * 32] = ef[k];

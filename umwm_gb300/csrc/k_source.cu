@@ -98,8 +98,12 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
   return s;
 }
 
+#ifndef UMWM_INTEG_MINB
+#define UMWM_INTEG_MINB 3  // resident CTAs per SM the register budget is sized for (two groups)
+#endif
+
 template <int G, int H, bool INTEG>
-__global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? 3 : 4))
+__global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? UMWM_INTEG_MINB : 4))
     k_source(const Params prm, const Ptrs P, int compute_rot) {
   constexpr int PW = 32 / G;   // points per warp
   constexpr int PPC = 4 * PW;  // points per CTA (4 warps)
