@@ -345,6 +345,8 @@ def run_surrogate(args):
 
     U.set_option("device", local_rank)
     U.surrogate_init(37, 36, seed=7)
+    U.set_option("surrogate_tol", args.sur_tol)
+    U.set_option("surrogate_tol_level", args.sur_tol_level)
     U.surrogate_capture(args.pairs, args.pts_per_substep)
     gen = []
     t0 = time.perf_counter()
@@ -448,8 +450,9 @@ def run_surrogate(args):
             "ms_per_step": sur["gpu_ms"] / max(sur["substeps"], 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16 (MLP) / f32 (spectrum)", "data": "synthetic",
             "config": {"workload": "surrogate: hurricane %dx%d dx=2km seed 5, %g h, JONSWAP Hs 0.2 m start; MLP "
-                                   "1344-512-512-1344 GELU bf16/f32-acc; energy-budget tolerances 0.02 (total), 0.1 "
-                                   "(level, wind-weighted)" % (args.size, args.size, args.hours),
+                                   "1344-512-512-1344 GELU bf16/f32-acc; energy-budget tolerances %g (total), %g "
+                                   "(level, wind-weighted)" % (args.size, args.size, args.hours, args.sur_tol,
+                                                               args.sur_tol_level),
                        "pairs": int(U.stat("surrogate_pairs")), "pair_sources": gen,
                        "train_steps": int(len(losses)), "batch": 8192},
             "plain": {"value": v_plain, "gpu_ms": plain["gpu_ms"], "substeps": plain["substeps"]},
@@ -547,6 +550,8 @@ def main():
     ap.add_argument("--pts-per-substep", type=int, default=16384)
     ap.add_argument("--train-steps", type=int, default=2000)
     ap.add_argument("--hours", type=float, default=12.0)
+    ap.add_argument("--sur-tol", type=float, default=0.02, help="surrogate total-energy budget per substep")
+    ap.add_argument("--sur-tol-level", type=float, default=0.1, help="surrogate per-level energy budget")
     ap.add_argument("--members", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
