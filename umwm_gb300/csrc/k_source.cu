@@ -99,11 +99,15 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
 }
 
 #ifndef UMWM_INTEG_MINB
-#define UMWM_INTEG_MINB 3  // resident CTAs per SM the register budget is sized for (two groups)
+#define UMWM_INTEG_MINB 3  // resident CTAs per SM the register budget is sized for (two groups);
+                           // 4 (128 registers, spills) measured 15 % slower
+#endif
+#ifndef UMWM_PHYS_MINB
+#define UMWM_PHYS_MINB 4
 #endif
 
 template <int G, int H, bool INTEG>
-__global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? UMWM_INTEG_MINB : 4))
+__global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? UMWM_INTEG_MINB : UMWM_PHYS_MINB))
     k_source(const Params prm, const Ptrs P, int compute_rot) {
   constexpr int PW = 32 / G;   // points per warp
   constexpr int PPC = 4 * PW;  // points per CTA (4 warps)
