@@ -55,8 +55,8 @@ __device__ __forceinline__ float sin_dir(const Params& prm, const WindIn& w, flo
 }
 
 #ifndef UMWM_ADVECT_MINB
-#define UMWM_ADVECT_MINB 4  // resident CTAs per SM the register budget is sized for (two groups);
-                            // 4 (128 registers, a few spilled) measured 9 % faster than 3 (168)
+#define UMWM_ADVECT_MINB 5  // resident CTAs per SM the register budget is sized for (two groups):
+                            // 96 registers with some spilling measured faster than 128 or 168
 #endif
 
 template <int G, int H, bool CURV>

@@ -103,7 +103,7 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
                            // 4 (128 registers, spills) measured 15 % slower
 #endif
 #ifndef UMWM_PHYS_MINB
-#define UMWM_PHYS_MINB 4
+#define UMWM_PHYS_MINB 5  // 96 registers, no spills; measured faster than 4 (128)
 #endif
 
 template <int G, int H, bool INTEG>
