@@ -102,6 +102,9 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
 #define UMWM_INTEG_MINB 3  // resident CTAs per SM the register budget is sized for (two groups);
                            // 4 (128 registers, spills) measured 15 % slower
 #endif
+#ifndef UMWM_INTEG_SMEM_LAGS
+#define UMWM_INTEG_SMEM_LAGS 0  // 1: the integration keeps its two lagged levels in shared memory
+#endif
 #ifndef UMWM_PHYS_MINB
 #define UMWM_PHYS_MINB 5  // 96 registers, no spills; measured faster than 4 (128)
 #endif
@@ -171,10 +174,21 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? UMWM_
 
   float A = 0.f, B = 0.f, C = 0.f;  // dummy coefficients of the current level
   float mx = 0.f, rmx = 0.f;
-  // the current level and the two previous ones (e and raw Sds per direction)
-  float ec[H], sc[H], e1[H], s1[H], e2[H], s2[H];
+  // the current level and the two previous ones (e and raw Sds per direction);
+  // with SL the previous two live in shared memory, slot = level & 1
+  constexpr bool SL = INTEG && UMWM_INTEG_SMEM_LAGS;
+  __shared__ float lag[SL ? 2 : 1][2][SL ? H : 1][128];
+  float ec[H], sc[H], e1[SL ? 1 : H], s1[SL ? 1 : H], e2[SL ? 1 : H], s2[SL ? 1 : H];
 #pragma unroll
-  for (int k = 0; k < H; ++k) { ec[k] = sc[k] = e1[k] = s1[k] = e2[k] = s2[k] = 0.f; }
+  for (int k = 0; k < H; ++k) ec[k] = sc[k] = 0.f;
+  if (!SL) {
+#pragma unroll
+    for (int k = 0; k < (SL ? 1 : H); ++k) e1[k] = s1[k] = e2[k] = s2[k] = 0.f;
+  }
+#define LAG_E1(k) (SL ? lag[(o - 1) & 1][0][SL ? (k) : 0][threadIdx.x] : e1[SL ? 0 : (k)])
+#define LAG_S1(k) (SL ? lag[(o - 1) & 1][1][SL ? (k) : 0][threadIdx.x] : s1[SL ? 0 : (k)])
+#define LAG_E2(k) (SL ? lag[o & 1][0][SL ? (k) : 0][threadIdx.x] : e2[SL ? 0 : (k)])
+#define LAG_S2(k) (SL ? lag[o & 1][1][SL ? (k) : 0][threadIdx.x] : s2[SL ? 0 : (k)])
   Coef Cc{}, C1{}, C2{};
 
   const int OL = INTEG ? O + 2 : OP;
@@ -266,11 +280,12 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? UMWM_
         for (int k = 0; k < H; ++k) {
           const float s = sin_k(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0,
                                 L2.fkovg, false);
-          const float snl = (L2.bf1r * s1[k]) * e1[k] + (L2.bf2r * sc[k]) * ec[k] - (prm.snl_fac * s2[k]) * e2[k];
-          const float S = s - s2[k] * L2.cothkd - L2.sbf - sdt - L2.sdv + sice;
-          const float ef = e2[k] * ex2a(dts * S * 1.44269504f) + dts * snl;
+          const float e2k = LAG_E2(k), s2k = LAG_S2(k);
+          const float snl = (L2.bf1r * LAG_S1(k)) * LAG_E1(k) + (L2.bf2r * sc[k]) * ec[k] - (prm.snl_fac * s2k) * e2k;
+          const float S = s - s2k * L2.cothkd - L2.sbf - sdt - L2.sdv + sice;
+          const float ef = e2k * ex2a(dts * S * 1.44269504f) + dts * snl;
           if (valid) {
-            ES[k * 32] = 0.5f * (e2[k] + ef);
+            ES[k * 32] = 0.5f * (LAG_E2(k) + ef);
             EF[k * 32] = ef;
           }
         }
@@ -290,7 +305,7 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? UMWM_
             ef = oneoverk4 * powp(num / den, prm.inv_sds_power);
           }
           if (valid) {
-            ES[k * 32] = 0.5f * (e2[k] + ef);
+            ES[k * 32] = 0.5f * (LAG_E2(k) + ef);
             EF[k * 32] = ef;
           }
         }
@@ -299,7 +314,15 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? UMWM_
 
     if (INTEG) {
 #pragma unroll
-      for (int k = 0; k < H; ++k) { e2[k] = e1[k]; s2[k] = s1[k]; e1[k] = ec[k]; s1[k] = sc[k]; }
+      for (int k = 0; k < H; ++k) {
+        if (SL) {  // level o replaces level o-2, finished above
+          lag[o & 1][0][SL ? k : 0][threadIdx.x] = ec[k];
+          lag[o & 1][1][SL ? k : 0][threadIdx.x] = sc[k];
+        } else {
+          e2[SL ? 0 : k] = e1[SL ? 0 : k]; s2[SL ? 0 : k] = s1[SL ? 0 : k];
+          e1[SL ? 0 : k] = ec[k]; s1[SL ? 0 : k] = sc[k];
+        }
+      }
       C2 = C1;
       C1 = Cc;
     }
