@@ -99,18 +99,19 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
 }
 
 #ifndef UMWM_INTEG_MINB
-#define UMWM_INTEG_MINB 3  // resident CTAs per SM the register budget is sized for (two groups);
-                           // 4 (128 registers, spills) measured 15 % slower
+#define UMWM_INTEG_MINB 4  // resident CTAs per SM the register budget is sized for (two groups);
+                           // with the lagged levels in shared memory: 122 registers, no spills
 #endif
 #ifndef UMWM_INTEG_SMEM_LAGS
-#define UMWM_INTEG_SMEM_LAGS 0  // 1: the integration keeps its two lagged levels in shared memory
+#define UMWM_INTEG_SMEM_LAGS 1  // the integration keeps its two lagged levels in shared memory
+                                // (37 KB per CTA): 3.56 ms instead of 4.28 ms with them in registers
 #endif
 #ifndef UMWM_PHYS_MINB
 #define UMWM_PHYS_MINB 5  // 96 registers, no spills; measured faster than 4 (128)
 #endif
 
 template <int G, int H, bool INTEG>
-__global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? UMWM_INTEG_MINB : UMWM_PHYS_MINB))
+__global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM_INTEG_SMEM_LAGS && H <= 18 ? UMWM_INTEG_MINB : 3) : UMWM_PHYS_MINB))
     k_source(const Params prm, const Ptrs P, int compute_rot) {
   constexpr int PW = 32 / G;   // points per warp
   constexpr int PPC = 4 * PW;  // points per CTA (4 warps)
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? UMWM_
   float mx = 0.f, rmx = 0.f;
   // the current level and the two previous ones (e and raw Sds per direction);
   // with SL the previous two live in shared memory, slot = level & 1
-  constexpr bool SL = INTEG && UMWM_INTEG_SMEM_LAGS;
+  constexpr bool SL = INTEG && UMWM_INTEG_SMEM_LAGS && H <= 18;  // within 48 KB of static shared memory
   __shared__ float lag[SL ? 2 : 1][2][SL ? H : 1][128];
   float ec[H], sc[H], e1[SL ? 1 : H], s1[SL ? 1 : H], e2[SL ? 1 : H], s2[SL ? 1 : H];
 #pragma unroll
