@@ -106,6 +106,9 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
 #define UMWM_INTEG_SMEM_LAGS 1  // the integration keeps its two lagged levels in shared memory
                                 // (37 KB per CTA): 3.56 ms instead of 4.28 ms with them in registers
 #endif
+#ifndef UMWM_INTEG_CW_FMA
+#define UMWM_INTEG_CW_FMA 0  // 1: the integration forms cos(wdir - th) as cos wdir cos th + sin wdir sin th
+#endif
 #ifndef UMWM_PHYS_MINB
 #define UMWM_PHYS_MINB 5  // 96 registers, no spills; measured faster than 4 (128)
 #endif
@@ -133,7 +136,8 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
   const float ra = G == 2 ? (q ? -1.f : 1.f) : (q == 0 ? 1.f : (q == 2 ? -1.f : 0.f));
   const float rb = G == 2 ? 0.f : (q == 1 ? 1.f : (q == 3 ? -1.f : 0.f));
   const float c2s = (G == 4 && (q & 1)) ? -1.f : 1.f;  // cos/sin(2 th) sign of the group
-  __shared__ float cws[H][128];
+  constexpr bool CWS = !(INTEG && UMWM_INTEG_CW_FMA);  // cos(wdir - th) table in shared memory
+  __shared__ float cws[CWS ? H : 1][128];
 
   const float dts = INTEG ? ctl->dts : 0.f;
   const float ustar = P.ustar[jj];
@@ -146,7 +150,11 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
   const float ucg = G == 2 ? ra * wi.uc : ra * wi.uc + rb * wi.vc;
   const float vcg = G == 2 ? ra * wi.vc : ra * wi.vc - rb * wi.uc;
 #pragma unroll
-  for (int k = 0; k < H; ++k) cws[k][threadIdx.x] = cosf(wdir - prm.th[q * H + k]);
+  for (int k = 0; k < (CWS ? H : 0); ++k) cws[CWS ? k : 0][threadIdx.x] = cosf(wdir - prm.th[q * H + k]);
+  // cos(wdir - th) = cwa cos th0 + cwb sin th0 in the group's frame
+  const float cw0 = cosf(wdir), sw0 = sinf(wdir);
+  const float cwa = ra * cw0 + rb * sw0, cwb = ra * sw0 - rb * cw0;
+#define CW(k) (CWS ? cws[CWS ? (k) : 0][threadIdx.x] : cwa * prm.cth[k] + cwb * prm.sth[k])
   // own bins only: no barrier needed (each thread reads its own column)
 
   int nie = N, niw = N, nin = N, nis = N;
@@ -237,7 +245,7 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
         const float sink = Lc.sbf + sdtc * Lc.kk + Lc.sdv - (sv != 0.f ? 2.f * Lc.cg0 * sv : 0.f);
 #pragma unroll
         for (int k = 0; k < H; ++k) {
-          const float s = sin_k(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], Lc.cp0,
+          const float s = sin_k(prm, wi, U, CW(k), ucg * prm.cth[k], vcg * prm.sth[k], Lc.cp0,
                                 Lc.fkovg, false);
           mx = fmaxf(mx, fabsf(s - sc[k] * cs - sink));
         }
@@ -279,7 +287,7 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
       if (prog) {
 #pragma unroll
         for (int k = 0; k < H; ++k) {
-          const float s = sin_k(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0,
+          const float s = sin_k(prm, wi, U, CW(k), ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0,
                                 L2.fkovg, false);
           const float e2k = LAG_E2(k), s2k = LAG_S2(k);
           const float snl = (L2.bf1r * LAG_S1(k)) * LAG_E1(k) + (L2.bf2r * sc[k]) * ec[k] - (prm.snl_fac * s2k) * e2k;
@@ -295,7 +303,7 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
         const float sAc = prm.twopisds_fac * prm.f[Lv];
 #pragma unroll
         for (int k = 0; k < H; ++k) {
-          const float s = sin_k(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0,
+          const float s = sin_k(prm, wi, U, CW(k), ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0,
                                 L2.fkovg, true);
           const float num = s - sdt - L2.sdv + sice;
           float ef = 0.f;
