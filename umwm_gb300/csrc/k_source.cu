@@ -108,6 +108,7 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
 #endif
 #ifndef UMWM_INTEG_CW_FMA
 #define UMWM_INTEG_CW_FMA 0  // 1: the integration forms cos(wdir - th) as cos wdir cos th + sin wdir sin th
+                             // (frees 9 KB of shared memory; measured no faster at 4, 5 or 6 CTAs)
 #endif
 #ifndef UMWM_PHYS_MINB
 #define UMWM_PHYS_MINB 5  // 96 registers, no spills; measured faster than 4 (128)
