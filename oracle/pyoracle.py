@@ -127,7 +127,10 @@ class Oracle:
     _WET = {"ar", "cd", "dxn", "dxs", "dye", "dyw", "fcutoff", "oneovar", "oneovdx", "oneovdy", "shelt",
             "physics_time_step", "ustar", "taux", "tauy", "taux_form", "tauy_form", "taux_skin", "tauy_skin",
             "taux_diag", "tauy_diag", "tailatmx", "tailatmy", "ht", "mss", "mwd", "mwl", "mwp", "dwd", "dwl",
-            "dwp", "dcp0", "dcp", "dcg0", "dcg", "momx", "momy", "cgmxx", "cgmxy", "cgmyy", "ds", "oc"}
+            "dwp", "dcp0", "dcp", "dcg0", "dcg", "momx", "momy", "cgmxx", "cgmxy", "cgmyy", "ds", "oc",
+            "taux_ocntop", "tauy_ocntop", "taux_ocnbot", "tauy_ocnbot", "taux_snl", "tauy_snl", "epsx_ocn",
+            "epsy_ocn", "epsx_atm", "epsy_atm", "tailocnx", "tailocny", "taux1", "tauy1", "taux2", "tauy2",
+            "taux3", "tauy3"}
     _IMM = {"mi", "ni", "iw", "ie", "is", "in", "iiw", "iie", "iis", "iin", "d", "dx", "dy", "wspd", "wdir",
             "uc", "vc", "rhoa", "rhow", "rhorat", "fice"}
     _TWOD = {"ii", "mask", "d_2d", "dx_2d", "dy_2d", "curv"}

@@ -219,6 +219,9 @@ struct Model {
   std::vector<T> e, ef, dummy, rotl, rotr, sds, snl, ssin;
   // stokes
   std::vector<T> depth, ds, us, vs, usmag, util;
+  // stress('ocn') outputs over wet points (index 1..im)
+  std::vector<T> taux_ocntop, tauy_ocntop, taux_ocnbot, tauy_ocnbot, taux_snl, tauy_snl, epsx_ocn, epsy_ocn,
+      epsx_atm, epsy_atm, tailocnx, tailocny, taux1, tauy1, taux2, tauy2, taux3, tauy3;
 
   // inputs standing in for files
   std::map<std::string, std::vector<float>> gridtopo;                        // lon, lat, z
@@ -1162,6 +1165,117 @@ struct Model {
     return u;
   }
 
+  // stress('ocn'), umwm_stress.F90:34-214: momentum and energy fluxes into
+  // the ocean from the current spectrum e and the source terms of the last
+  // source() call (ssin, sds after the cothkd factor, snl, sdt).
+  void stress_ocn() {
+    for (auto* v : {&taux_ocntop, &tauy_ocntop, &taux_ocnbot, &tauy_ocnbot, &taux_snl, &tauy_snl, &epsx_ocn,
+                    &epsy_ocn, &epsx_atm, &epsy_atm, &tailocnx, &tailocny, &taux1, &tauy1, &taux2, &tauy2,
+                    &taux3, &tauy3})
+      v->assign(im + 1, T(0));
+#pragma omp parallel for schedule(static)
+    for (int q = istart; q <= iend; ++q) {
+      const T tail = stress_tail(wspd[q], k[oi(om, q)]);
+      std::vector<T> ux(om + 1), uy(om + 1);
+      auto integrate = [&](T& sx, T& sy) {  // sum(util(:,i) * kdk(:,i)) * rhow * dthg, o in order
+        T ax = 0, ay = 0;
+        for (int o = 1; o <= om; ++o) {
+          ax = ax + ux[o] * kdk[oi(o, q)];
+          ay = ay + uy[o] * kdk[oi(o, q)];
+        }
+        sx = ax * rhow[q] * dthg;
+        sy = ay * rhow[q] * dthg;
+      };
+      auto clear = [&] { std::fill(ux.begin(), ux.end(), T(0)); std::fill(uy.begin(), uy.end(), T(0)); };
+      // stress into the ocean top (:39-80)
+      clear();
+      for (int p = 1; p <= pm; ++p) {
+        for (int o = 1; o <= om; ++o) {
+          const size_t a = opi(o, p, q), b = oi(o, q);
+          ux[o] = ux[o] + e[a] * (sds[a] + sdt[b] + sdv[b]) * cth[p - 1] * invcp0[b];
+          uy[o] = uy[o] + e[a] * (sds[a] + sdt[b] + sdv[b]) * sth[p - 1] * invcp0[b];
+        }
+        for (int o = 3; o <= om; ++o) {
+          const size_t a = opi(o, p, q), b = oi(o, q);
+          const T w = bf1 * cp0[b] * invcp0[oi(o - 1, q)] + bf2 * cp0[b] * invcp0[oi(o - 2, q)];
+          ux[o] = ux[o] - snl[a] * w * cth[p - 1] * invcp0[b];
+          uy[o] = uy[o] - snl[a] * w * sth[p - 1] * invcp0[b];
+        }
+      }
+      tailocnx[q] = ux[om] * k[oi(om, q)] * tail * rhow[q] * dthg;
+      tailocny[q] = uy[om] * k[oi(om, q)] * tail * rhow[q] * dthg;
+      integrate(taux_ocntop[q], tauy_ocntop[q]);
+      taux_ocntop[q] = taux_ocntop[q] + tailocnx[q] + taux_skin[q];
+      tauy_ocntop[q] = tauy_ocntop[q] + tailocny[q] + tauy_skin[q];
+      // stress into the ocean bottom (:95-108)
+      clear();
+      for (int p = 1; p <= pm; ++p)
+        for (int o = 1; o <= om; ++o) {
+          const size_t a = opi(o, p, q), b = oi(o, q);
+          ux[o] = ux[o] + e[a] * sbf[b] * cth[p - 1] * invcp0[b];
+          uy[o] = uy[o] + e[a] * sbf[b] * sth[p - 1] * invcp0[b];
+        }
+      integrate(taux_ocnbot[q], tauy_ocnbot[q]);
+      // momentum lost by the downshifting (:110-128)
+      clear();
+      for (int p = 1; p <= pm; ++p)
+        for (int o = 3; o <= oc[q]; ++o) {
+          const size_t a = opi(o, p, q), b = oi(o, q);
+          const T w = bf1 * (1 - cp0[b] * invcp0[oi(o - 1, q)]) + bf2 * (1 - cp0[b] * invcp0[oi(o - 2, q)]);
+          ux[o] = ux[o] + snl[a] * w * cth[p - 1] * invcp0[b];
+          uy[o] = uy[o] + snl[a] * w * sth[p - 1] * invcp0[b];
+        }
+      integrate(taux_snl[q], tauy_snl[q]);
+      // energy flux into the ocean (:130-157)
+      clear();
+      for (int p = 1; p <= pm; ++p) {
+        for (int o = 1; o <= om; ++o) {
+          const size_t a = opi(o, p, q);
+          ux[o] = ux[o] + e[a] * sds[a] * cth[p - 1];
+          uy[o] = uy[o] + e[a] * sds[a] * sth[p - 1];
+        }
+        for (int o = 3; o <= om; ++o) {
+          const size_t a = opi(o, p, q), b = oi(o, q);
+          const T w = bf1 * cp0[b] * invcp0[oi(o - 1, q)] + bf2 * cp0[b] * invcp0[oi(o - 2, q)];
+          ux[o] = ux[o] - snl[a] * w * cth[p - 1];
+          uy[o] = uy[o] - snl[a] * w * sth[p - 1];
+        }
+      }
+      integrate(epsx_ocn[q], epsy_ocn[q]);
+      // energy flux from the air (:159-172)
+      clear();
+      for (int p = 1; p <= pm; ++p)
+        for (int o = 1; o <= om; ++o) {
+          const size_t a = opi(o, p, q);
+          ux[o] = ux[o] + e[a] * ssin[a] * cth[p - 1];
+          uy[o] = uy[o] + e[a] * ssin[a] * sth[p - 1];
+        }
+      integrate(epsx_atm[q], epsy_atm[q]);
+      // form drag by wind pushing waves (1), waves against wind (2), waves
+      // overrunning wind (3) (:174-212)
+      T a1x = 0, a1y = 0, a2x = 0, a2y = 0, a3x = 0, a3y = 0;
+      for (int p = 1; p <= pm; ++p)
+        for (int o = 1; o <= om; ++o) {
+          const size_t a = opi(o, p, q), b = oi(o, q);
+          const T dd = e[a] * ssin[a] * invcp0[b] * kdk[b];
+          dummy[a] = dd;
+          if (ssin[a] > 0) {
+            a1x = a1x + dd * cth[p - 1];
+            a1y = a1y + dd * sth[p - 1];
+          } else if (std::cos(wdir[q] - th[p - 1]) < 0) {
+            a2x = a2x + dd * cth[p - 1];
+            a2y = a2y + dd * sth[p - 1];
+          } else {
+            a3x = a3x + dd * cth[p - 1];
+            a3y = a3y + dd * sth[p - 1];
+          }
+        }
+      taux1[q] = a1x * rhow[q] * dthg; tauy1[q] = a1y * rhow[q] * dthg;
+      taux2[q] = a2x * rhow[q] * dthg; tauy2[q] = a2y * rhow[q] * dthg;
+      taux3[q] = a3x * rhow[q] * dthg; tauy3[q] = a3y * rhow[q] * dthg;
+    }
+  }
+
   void stress_atm() {
 #pragma omp parallel for schedule(static)
     for (int q = istart; q <= iend; ++q) {
@@ -1368,6 +1482,7 @@ struct Model {
       if (firstdtg) firstdtg = false;
       if (stokes) stokes_drift();
       diag();
+      stress_ocn();  // every outer step (the reference calls it before gridded output)
     }
     return true;
   }
@@ -1383,9 +1498,9 @@ struct Handle {
 template <typename M>
 bool get_field(M& m, const std::string& name, double* out, long n) {
   using T = typename std::remove_reference<decltype(m.dts)>::type;
-  auto copy_wet = [&](const std::vector<T>& v) {  // (1..im)
+  auto copy_wet = [&](const std::vector<T>& v) {  // (1..im); zeros before the array is first computed
     if (n < m.im) return false;
-    for (int q = 1; q <= m.im; ++q) out[q - 1] = (double)v[q];
+    for (int q = 1; q <= m.im; ++q) out[q - 1] = q < (int)v.size() ? (double)v[q] : 0.0;
     return true;
   };
   auto copy_imm = [&](const std::vector<T>& v) {
@@ -1482,7 +1597,12 @@ bool get_field(M& m, const std::string& name, double* out, long n) {
       {"ar", &m.ar}, {"cd", &m.cd}, {"dxn", &m.dxn}, {"dxs", &m.dxs}, {"dye", &m.dye}, {"dyw", &m.dyw},
       {"fcutoff", &m.fcutoff}, {"oneovar", &m.oneovar}, {"oneovdx", &m.oneovdx}, {"oneovdy", &m.oneovdy},
       {"shelt", &m.shelt}, {"physics_time_step", &m.physics_time_step}, {"ustar", &m.ustar}, {"taux", &m.taux},
-      {"tauy", &m.tauy}, {"taux_form", &m.taux_form}, {"tauy_form", &m.tauy_form}, {"taux_skin", &m.taux_skin},
+      {"tauy", &m.tauy}, {"taux_form", &m.taux_form}, {"tauy_form", &m.tauy_form}, {"taux_skin", &m.taux_skin}, {"taux_ocntop", &m.taux_ocntop},
+      {"tauy_ocntop", &m.tauy_ocntop}, {"taux_ocnbot", &m.taux_ocnbot}, {"tauy_ocnbot", &m.tauy_ocnbot},
+      {"taux_snl", &m.taux_snl}, {"tauy_snl", &m.tauy_snl}, {"epsx_ocn", &m.epsx_ocn}, {"epsy_ocn", &m.epsy_ocn},
+      {"epsx_atm", &m.epsx_atm}, {"epsy_atm", &m.epsy_atm}, {"tailocnx", &m.tailocnx}, {"tailocny", &m.tailocny},
+      {"taux1", &m.taux1}, {"tauy1", &m.tauy1}, {"taux2", &m.taux2}, {"tauy2", &m.tauy2}, {"taux3", &m.taux3},
+      {"tauy3", &m.tauy3},
       {"tauy_skin", &m.tauy_skin}, {"taux_diag", &m.taux_diag}, {"tauy_diag", &m.tauy_diag},
       {"tailatmx", &m.tailatmx}, {"tailatmy", &m.tailatmy}, {"ht", &m.ht}, {"mss", &m.mss}, {"mwd", &m.mwd},
       {"mwl", &m.mwl}, {"mwp", &m.mwp}, {"dwd", &m.dwd}, {"dwl", &m.dwl}, {"dwp", &m.dwp}, {"dcp0", &m.dcp0},
