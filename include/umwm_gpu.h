@@ -153,7 +153,12 @@ int umwm_gpu_write_restart(const char* path);
  * wdir, uc, vc, rhoa, rhow, rhorat, fice, d, dx, dy), Stokes drift 'us',
  * 'vs' (lm*im, level-major), spectral tables (om*im: k, kdk, k3dk, ...;
  * cp0, cg0 as om*(im+1) with the ghost point first), 'f' (om), 'th' (pm),
- * 'depth' (lm) and the scalars dts, dta, dtr, dtamin, sumt, cgmax, dth. */
+ * 'depth' (lm) and the scalars dts, dta, dtr, dtamin, sumt, cgmax, dth.
+ * The outputs of stress('ocn') (umwm_stress.F90:34-214), over wet points,
+ * once it has run (option "stress_ocn", or an outer step with gridded
+ * output due): taux_ocntop, tauy_ocntop, taux_ocnbot, tauy_ocnbot, taux_snl,
+ * tauy_snl, epsx_ocn, epsy_ocn, epsx_atm, epsy_atm, tailocnx, tailocny,
+ * taux1, tauy1, taux2, tauy2, taux3, tauy3. */
 int umwm_gpu_get_field(const char* name, float* out, long n);
 
 /* Integer fields: mask, ii (mm*nm); mi, ni, iw, ie, is, in, iiw, iie,
@@ -175,6 +180,8 @@ int umwm_gpu_get_screen(double* out, long n, long* rows);
  * substep; results are bit-identical), "kernel_timing" (CUDA-event time of
  * each kernel, read with umwm_gpu_get_stat "ms:<kernel>"; the inner loop
  * then runs host-driven), "device" (CUDA device of the next initialize),
+ * "stress_ocn" (run stress('ocn') after every outer step: the last substep
+ * of each step keeps its source terms, three more spectrum-sized arrays),
  * "direction_groups" (2, default: each point's directions in two half-turn
  * groups per warp lane pair; 4: four quarter-turn groups, fewer registers
  * per thread; needs pm % 4 == 0 and pm/4 in {4, 6, 8, 9, 12}; results differ

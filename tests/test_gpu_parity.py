@@ -206,3 +206,33 @@ def test_direction_groups_random_field(U, oracle_mod, groups):
     o = run_oracle(oracle_mod, case, 32, max_substeps=8)
     _compare_state(U, o, 1e-4, FIELD_TOL)
     U.umwm_finalize()
+
+
+OCN_PAIRS = [("taux_ocntop", "tauy_ocntop"), ("taux_ocnbot", "tauy_ocnbot"), ("taux_snl", "tauy_snl"),
+             ("epsx_ocn", "epsy_ocn"), ("epsx_atm", "epsy_atm"), ("tailocnx", "tailocny"), ("taux1", "tauy1"),
+             ("taux2", "tauy2"), ("taux3", "tauy3")]
+
+
+@pytest.mark.parametrize("which", ["hurricane", "random_field"])
+def test_stress_ocn_vs_oracle(U, oracle_mod, which):
+    """stress('ocn') after full outer steps: ocean-top and bottom stress, the
+    momentum lost by downshifting, energy fluxes to the ocean and from the
+    air, and the three form-drag parts, against the fp32 oracle (each vector
+    to 1e-3 of its largest magnitude)."""
+    from umwm_gb300 import configs
+
+    if which == "hurricane":
+        case = configs.hurricane(mm=40, nm=36, hours=1, dx=4000.0, dtg=600, seed=3)
+    else:
+        case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0)
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=case.nml)
+    U.set_option("stress_ocn", 1)
+    U.umwm_run(case.start, case.stop)
+    got = {n: U.get_field(n) for pair in OCN_PAIRS for n in pair}
+    U.umwm_finalize()
+    o = run_oracle(oracle_mod, case, 32)
+    for nx, ny in OCN_PAIRS:
+        e = vec_err(got[nx], got[ny], o.get(nx), o.get(ny))
+        assert e < 1e-3, "(%s, %s) err %.3g of max" % (nx, ny, e)

@@ -60,6 +60,7 @@ struct Params {
   const int* tile_mem;   // member of each tile [ntiles]
   float g, explim, sin_fac, fieldscale1, fieldscale2, twopisds_fac, sds_power, inv_sds_power, mss_fac, snl_fac,
       sdt_fac, z, nu_air, kappa, fprog, dth, dthg, oneovdth, dtg, fice_lth, fice_uth, eulerinv, rhow0;
+  float bf1, bf2;  // downshifting weights (umwm_init.F90:1290-1294)
   int winds, currents, air_density, water_density, seaice, restart, curvilinear, isglobal;
   int ice_possible;  // fice can exceed fice_lth somewhere
   int groups4;       // spectral kernels use 4 quarter-turn direction groups (option "direction_groups")
@@ -104,6 +105,7 @@ struct Global {
   int budget;              // substeps the graph-driven inner loop may still run (-1: no limit)
   int iters;               // substeps the graph-driven inner loop ran since it was armed
   int nonfinite;           // non-finite values found by the last finite check
+  int save_src;            // the last substep of this dtg keeps its source terms (for stress('ocn'))
 };
 
 struct Ptrs {
@@ -136,6 +138,18 @@ struct Ptrs {
   // tiles with fb_tile[t] != 0 and writes only points with fb_pt[j] != 0
   const int* fb_tile;
   const unsigned char* fb_pt;
+  // source terms of the last substep of a dtg, kept for stress('ocn') when
+  // Global::save_src is set (null when not allocated): Sin, Sds after the
+  // cothkd factor, Snl (spectrum layout) and the ustar they used [ldN]
+  float *src_sin, *src_sds, *src_snl, *src_ust;
+  float* ocn;  // stress('ocn') outputs, OCN_COUNT arrays of [ldN]
+};
+
+// stress('ocn') outputs (umwm_stress.F90:34-214), in this order in Ptrs::ocn
+enum OcnField {
+  OCN_TAUX_TOP = 0, OCN_TAUY_TOP, OCN_TAUX_BOT, OCN_TAUY_BOT, OCN_TAUX_SNL, OCN_TAUY_SNL, OCN_EPSX_OCN,
+  OCN_EPSY_OCN, OCN_EPSX_ATM, OCN_EPSY_ATM, OCN_TAILX, OCN_TAILY, OCN_TAUX1, OCN_TAUY1, OCN_TAUX2, OCN_TAUY2,
+  OCN_TAUX3, OCN_TAUY3, OCN_COUNT
 };
 
 // element offsets in the blocked layouts

@@ -69,6 +69,14 @@ __device__ __forceinline__ float sin_bin(const Params& prm, const WindIn& w, flo
   return s;
 }
 
+// stress_tail, umwm_stress.F90:300-311
+__device__ __forceinline__ float stress_tail(float w, float kmax) {
+  const float kcap = 1e3f, a = 0.000112f, b = -0.01451f, c = -1.0186f;
+  float tail = a * (w * w) + b * w + c;
+  float kpt = powf(kmax, tail);
+  return (powf(kcap, tail + 1.f) - kmax * kpt) / (kpt * (tail + 1.f));
+}
+
 // Bounded spin on a device flag is never used; all cross-block ordering is
 // by kernel boundaries on one stream.
 

@@ -31,14 +31,6 @@ __device__ __forceinline__ void bulk_prefetch(const void* p, unsigned bytes) {
   asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
-// stress_tail, umwm_stress.F90:300-311
-__device__ __forceinline__ float stress_tail(float w, float kmax) {
-  const float kcap = 1e3f, a = 0.000112f, b = -0.01451f, c = -1.0186f;
-  float tail = a * (w * w) + b * w + c;
-  float kpt = powf(kmax, tail);
-  return (powf(kcap, tail + 1.f) - kmax * kpt) / (kpt * (tail + 1.f));
-}
-
 // Sin at one direction (same expression as the source kernels)
 __device__ __forceinline__ float sin_dir(const Params& prm, const WindIn& w, float U, float cw, float ucs, float vss,
                                          float cp0, float fkovg, bool tail) {

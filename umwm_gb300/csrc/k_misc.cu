@@ -314,6 +314,102 @@ __global__ void k_begin_dtg(const Params prm) {
   }
 }
 
+// stress('ocn'), umwm_stress.F90:34-214: per wet point, from the current
+// spectrum and the source terms the last substep of the dtg kept (Sin, Sds
+// after cothkd, Snl, and the ustar of its sdt).  One thread per point; the
+// sums over directions run inside the frequency sums in the reference's
+// order (p outer, o inner per accumulator, then the sum over o with kdk).
+__global__ void k_stress_ocn(const Params prm, const Ptrs P) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= prm.Ntot) return;
+  const Member& M = prm.mem[prm.tile_mem[j / TILE]];
+  if (j >= M.ghost) return;
+  const int ja = apt(M, j);
+  const int O = prm.O, NP = prm.P, oc = P.oc[j];
+  const float rhow = P.rhow[ja], wdir = P.wdir[ja];
+  const float sdtc = (prm.sdt_fac * sqrtf(P.rhorat[ja])) * P.src_ust[j];
+  auto tab = [&](int t, int o) { return P.TAB[tidx(prm, o, t, j)]; };
+  float top_x = 0, top_y = 0, bot_x = 0, bot_y = 0, snl_x = 0, snl_y = 0, eo_x = 0, eo_y = 0, ea_x = 0, ea_y = 0;
+  float tailx = 0, taily = 0;
+  float f1x = 0, f1y = 0, f2x = 0, f2y = 0, f3x = 0, f3y = 0;
+  for (int o = 0; o < O; ++o) {
+    const float cp0 = tab(T_CP0, o), icp = 1.f / cp0, kdk = tab(T_KDK, o), kk = tab(T_K, o);
+    const float sdt = sdtc * kk, sdv = tab(T_SDV, o), sbf = tab(T_SBF, o);
+    // downshifting weights at levels o >= 3 (1-based)
+    float wm = 0.f, wl = 0.f;
+    if (o >= 2) {
+      const float i1 = 1.f / tab(T_CP0, o - 1), i2 = 1.f / tab(T_CP0, o - 2);
+      wm = prm.bf1 * cp0 * i1 + prm.bf2 * cp0 * i2;
+      wl = prm.bf1 * (1.f - cp0 * i1) + prm.bf2 * (1.f - cp0 * i2);
+    }
+    float ux = 0, uy = 0, bx = 0, by = 0, nx = 0, ny = 0, ex = 0, ey = 0, ax = 0, ay = 0;
+    for (int p = 0; p < NP; ++p) {
+      const size_t a = sidx(prm, o, p, j);
+      const float e = P.E[a], sin_ = P.src_sin[a], sds = P.src_sds[a], snl = P.src_snl[a];
+      const float c = prm.cth[p], s = prm.sth[p];
+      ux = ux + e * (sds + sdt + sdv) * c * icp;
+      uy = uy + e * (sds + sdt + sdv) * s * icp;
+      if (o >= 2) {
+        ux = ux - snl * wm * c * icp;
+        uy = uy - snl * wm * s * icp;
+      }
+      bx = bx + e * sbf * c * icp;
+      by = by + e * sbf * s * icp;
+      if (o >= 2 && o < oc) {
+        nx = nx + snl * wl * c * icp;
+        ny = ny + snl * wl * s * icp;
+      }
+      ex = ex + e * sds * c;
+      ey = ey + e * sds * s;
+      if (o >= 2) {
+        ex = ex - snl * wm * c;
+        ey = ey - snl * wm * s;
+      }
+      ax = ax + e * sin_ * c;
+      ay = ay + e * sin_ * s;
+      const float dd = e * sin_ * icp * kdk;
+      if (sin_ > 0.f) {
+        f1x += dd * c; f1y += dd * s;
+      } else if (cosf(wdir - prm.th[p]) < 0.f) {
+        f2x += dd * c; f2y += dd * s;
+      } else {
+        f3x += dd * c; f3y += dd * s;
+      }
+    }
+    top_x += ux * kdk; top_y += uy * kdk;
+    bot_x += bx * kdk; bot_y += by * kdk;
+    snl_x += nx * kdk; snl_y += ny * kdk;
+    eo_x += ex * kdk; eo_y += ey * kdk;
+    ea_x += ax * kdk; ea_y += ay * kdk;
+    if (o == O - 1) {
+      const float tl = stress_tail(P.wspd[ja], kk);
+      tailx = ux * kk * tl * rhow * prm.dthg;
+      taily = uy * kk * tl * rhow * prm.dthg;
+    }
+  }
+  const float rg = rhow * prm.dthg;
+  const size_t L = (size_t)prm.ldN;
+  float* out = P.ocn;
+  out[OCN_TAUX_TOP * L + j] = top_x * rg + tailx + P.taux_skin[j];
+  out[OCN_TAUY_TOP * L + j] = top_y * rg + taily + P.tauy_skin[j];
+  out[OCN_TAUX_BOT * L + j] = bot_x * rg;
+  out[OCN_TAUY_BOT * L + j] = bot_y * rg;
+  out[OCN_TAUX_SNL * L + j] = snl_x * rg;
+  out[OCN_TAUY_SNL * L + j] = snl_y * rg;
+  out[OCN_EPSX_OCN * L + j] = eo_x * rg;
+  out[OCN_EPSY_OCN * L + j] = eo_y * rg;
+  out[OCN_EPSX_ATM * L + j] = ea_x * rg;
+  out[OCN_EPSY_ATM * L + j] = ea_y * rg;
+  out[OCN_TAILX * L + j] = tailx;
+  out[OCN_TAILY * L + j] = taily;
+  out[OCN_TAUX1 * L + j] = f1x * rg;
+  out[OCN_TAUY1 * L + j] = f1y * rg;
+  out[OCN_TAUX2 * L + j] = f2x * rg;
+  out[OCN_TAUY2 * L + j] = f2y * rg;
+  out[OCN_TAUX3 * L + j] = f3x * rg;
+  out[OCN_TAUY3 * L + j] = f3y * rg;
+}
+
 // Graph-driven inner loop: arm before the graph launch, then after each
 // substep count it and set the while node's condition (another substep while
 // a member is inside the dtg and the budget lasts).
@@ -384,6 +480,10 @@ cudaError_t launch_from_ref(const Params& prm, const float* F, float* E, int off
 }
 cudaError_t launch_begin_dtg(const Params& prm, cudaStream_t st) {
   k_begin_dtg<<<1, 256, 0, st>>>(prm);
+  return cudaGetLastError();
+}
+cudaError_t launch_stress_ocn(const Params& prm, const Ptrs& P, cudaStream_t st) {
+  k_stress_ocn<<<(prm.Ntot + 127) / 128, 128, 0, st>>>(prm, P);
   return cudaGetLastError();
 }
 cudaError_t launch_loop_arm(Global* g, int budget, cudaStream_t st) {

@@ -141,7 +141,10 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
   __shared__ float cws[CWS ? H : 1][128];
 
   const float dts = INTEG ? ctl->dts : 0.f;
+  // the last substep of the dtg keeps its source terms when stress('ocn') is due
+  const bool save = INTEG && P.src_sin && ctl->done && P.glob->save_src;
   const float ustar = P.ustar[jj];
+  if (save && valid && q == 0) P.src_ust[j] = ustar;  // the ustar of this substep's sdt
   const WindIn wi = load_wind(prm, P, jj, ja, ustar);
   const float wdir = P.wdir[ja];
   const float sdtc = (prm.sdt_fac * sqrtf(P.rhorat[ja])) * ustar;
@@ -285,6 +288,7 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
       const float sice = sv != 0.f ? 2.f * L2.cg0 * sv : 0.f;
       float* ES = P.ES + sidx(prm, 0, q * H, jj) + (size_t)Lv * lstride;
       float* EF = P.EF + sidx(prm, 0, q * H, jj) + (size_t)Lv * lstride;
+      const size_t so = sidx(prm, 0, q * H, jj) + (size_t)Lv * lstride;  // saved source terms
       if (prog) {
 #pragma unroll
         for (int k = 0; k < H; ++k) {
@@ -297,6 +301,11 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
           if (valid) {
             ES[k * 32] = 0.5f * (LAG_E2(k) + ef);
             EF[k * 32] = ef;
+            if (save) {
+              P.src_sin[so + k * 32] = s;
+              P.src_sds[so + k * 32] = s2k * L2.cothkd;
+              P.src_snl[so + k * 32] = snl;
+            }
           }
         }
       } else {
@@ -317,6 +326,11 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
           if (valid) {
             ES[k * 32] = 0.5f * (LAG_E2(k) + ef);
             EF[k * 32] = ef;
+            if (save) {
+              P.src_sin[so + k * 32] = s;
+              P.src_sds[so + k * 32] = LAG_S2(k) * L2.cothkd;
+              P.src_snl[so + k * 32] = 0.f;  // snl is zero above the cut-off
+            }
           }
         }
       }

@@ -19,6 +19,7 @@ cudaError_t launch_screen(const Params& prm, const Ptrs& P, cudaStream_t st);
 cudaError_t launch_to_ref(const Params& prm, const float* E, float* F, int off, int n, cudaStream_t st);
 cudaError_t launch_from_ref(const Params& prm, const float* F, float* E, int off, int n, cudaStream_t st);
 cudaError_t launch_begin_dtg(const Params& prm, cudaStream_t st);
+cudaError_t launch_stress_ocn(const Params& prm, const Ptrs& P, cudaStream_t st);
 cudaError_t launch_loop_arm(Global* g, int budget, cudaStream_t st);
 cudaError_t launch_loop_cond(Global* g, cudaGraphConditionalHandle h, cudaStream_t st);
 cudaError_t launch_count_nonfinite(const float* a, size_t n, int* count, cudaStream_t st);

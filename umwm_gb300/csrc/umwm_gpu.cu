@@ -104,6 +104,7 @@ struct Model {
   bool first = true;
   long long substeps = 0, max_substeps = -1;
   bool verbose = false, check_finite = false, use_graph = false;
+  bool ocn_every = false;  // stress('ocn') after every outer step (option "stress_ocn")
   double last_gpu_ms = 0, last_bins = 0;
   long long launches = 0;
   int sel = 0;      // member the getters and setters act on
@@ -341,6 +342,7 @@ int setup_params(Model& M) {
   p.g = H.g; p.explim = H.explim; p.sin_fac = H.sin_fac; p.fieldscale1 = H.fieldscale1;
   p.fieldscale2 = H.fieldscale2; p.twopisds_fac = H.twopisds_fac; p.sds_power = H.sds_power;
   p.inv_sds_power = H.inv_sds_power; p.mss_fac = H.mss_fac; p.snl_fac = H.snl_fac; p.sdt_fac = H.sdt_fac;
+  p.bf1 = H.bf1; p.bf2 = H.bf2;
   p.z = H.z; p.nu_air = H.nu_air; p.kappa = H.kappa; p.fprog = H.fprog; p.dth = H.dth; p.dthg = H.dthg;
   p.oneovdth = H.oneovdth; p.dtg = H.dtg; p.fice_lth = H.fice_lth; p.fice_uth = H.fice_uth;
   p.eulerinv = H.eulerinv; p.rhow0 = H.rhow0;
@@ -668,6 +670,23 @@ int check_ctl(Model& M) {
   return UMWM_OK;
 }
 
+// Buffers of stress('ocn'): the last substep's source terms and the outputs.
+// Allocated on first use; a captured inner loop holds the old pointers and is
+// rebuilt.
+int ensure_ocn(Model& M) {
+  if (M.P.src_sin) return UMWM_OK;
+  const size_t spec = (size_t)M.prm.O * M.prm.P * M.prm.ldN;
+  Dev& D = *M.dev;
+  CU(D.alloc(&M.P.src_sin, spec, false));
+  CU(D.alloc(&M.P.src_sds, spec, false));
+  CU(D.alloc(&M.P.src_snl, spec, false));
+  CU(D.alloc(&M.P.src_ust, (size_t)M.prm.ldN));
+  CU(D.alloc(&M.P.ocn, (size_t)OCN_COUNT * M.prm.ldN));
+  if (M.graph_exec) { cudaGraphExecDestroy(M.graph_exec); M.graph_exec = nullptr; }
+  if (M.graph) { cudaGraphDestroy(M.graph); M.graph = nullptr; }
+  return UMWM_OK;
+}
+
 // Enqueue the launches of one substep: prep, [sice], phys, dts, integ,
 // advect, [diag on the first substep of a run], screen.
 int enqueue_substep(Model& M, int compute_rot, int first, bool diag) {
@@ -807,6 +826,16 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     for (MemberHost& mh : M.mem)
       if ((rc = forcing_input(M, mh, cur))) return rc;
     CU(launch_begin_dtg(M.prm, M.st));  // sumt = 0, done = 0 for every member
+    // stress('ocn') is due after this step (umwm_top.F90:160-171)
+    const HostModel& H0 = M.mem[0].H;
+    const int64_t sod = now % 86400;
+    const bool grid_due = (H0.outgrid > 0 && (sod / 3600) % H0.outgrid == 0 && sod % 3600 == 0) || H0.outgrid == -1;
+    const bool ocn_due = M.ocn_every || (grid_due && M.P.src_sin);
+    if (ocn_due) {
+      if ((rc = ensure_ocn(M))) return rc;
+      static const int one = 1;
+      CU(cudaMemcpyAsync(&M.d_glob->save_src, &one, sizeof(int), cudaMemcpyHostToDevice, M.st));
+    }
     for (long long inner = 0;;) {
       if (inner > 10000000LL) return fail(UMWM_ERR_TIMEOUT, "umwm_run: more than 1e7 substeps in one dtg (dts stuck at 0?)");
       if (M.max_substeps >= 0 && M.substeps >= M.max_substeps) return finish_run(M);
@@ -838,6 +867,12 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     }
     CU(timed(M, K_DIAG, [&] { return launch_diag(M.prm, M.P, M.st); }));
     M.launches++;
+    if (ocn_due) {
+      static const int zero = 0;
+      CU(launch_stress_ocn(M.prm, M.P, M.st));
+      CU(cudaMemcpyAsync(&M.d_glob->save_src, &zero, sizeof(int), cudaMemcpyHostToDevice, M.st));
+      M.launches++;
+    }
     if (M.verbose) print_screen(M);
     // restart output, umwm_top.F90:183-190 (with the reference's test of
     // outspec == -1 for writing every step)
@@ -1290,6 +1325,16 @@ int umwm_gpu_get_field(const char* name, float* out, long n) {
       CU(cudaMemcpy(out, wetptrs[q] + mh.off, (size_t)N * 4, cudaMemcpyDeviceToHost));
       return UMWM_OK;
     }
+  static const char* ocnnames[OCN_COUNT] = {"taux_ocntop", "tauy_ocntop", "taux_ocnbot", "tauy_ocnbot", "taux_snl",
+                                            "tauy_snl", "epsx_ocn", "epsy_ocn", "epsx_atm", "epsy_atm", "tailocnx",
+                                            "tailocny", "taux1", "tauy1", "taux2", "tauy2", "taux3", "tauy3"};
+  for (int q = 0; q < OCN_COUNT; ++q)
+    if (s == ocnnames[q]) {
+      if (!P.ocn) return fail(UMWM_ERR_STATE, "get_field: " + s + " needs stress('ocn') (option stress_ocn or outgrid)");
+      if (need(N)) return UMWM_ERR_ARG;
+      CU(cudaMemcpy(out, P.ocn + (size_t)q * M->prm.ldN + mh.off, (size_t)N * 4, cudaMemcpyDeviceToHost));
+      return UMWM_OK;
+    }
   static const char* allnames[] = {"wspd", "wdir", "uc", "vc", "rhoa", "rhow", "rhorat", "fice"};
   float* const allptrs[] = {P.wspd, P.wdir, P.uc, P.vc, P.rhoa, P.rhow, P.rhorat, P.fice};
   for (size_t q = 0; q < 8; ++q)
@@ -1395,6 +1440,10 @@ int umwm_gpu_set_option(const char* name, double value) {
   if (s == "max_substeps") { M->max_substeps = (long long)value; return UMWM_OK; }
   if (s == "check_finite") { M->check_finite = value != 0; return UMWM_OK; }
   if (s == "use_graph") { M->use_graph = value != 0; return UMWM_OK; }
+  if (s == "stress_ocn") {
+    M->ocn_every = value != 0;
+    return M->ocn_every ? ensure_ocn(*M) : UMWM_OK;
+  }
   if (s == "direction_groups") {
     if (value != 2 && value != 4) return fail(UMWM_ERR_ARG, "direction_groups must be 2 or 4");
     if (value == 4 && !quarter_groups(M->prm.P))

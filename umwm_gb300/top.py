@@ -118,7 +118,9 @@ def stat(name):
 _WET = {"ustar", "cd", "taux", "tauy", "taux_form", "tauy_form", "taux_skin", "tauy_skin", "taux_diag",
         "tauy_diag", "tailatmx", "tailatmy", "shelt", "fcutoff", "physics_time_step", "ds", "ht", "mwp", "mwd",
         "mss", "mwl", "dwd", "dwl", "dwp", "dcp0", "dcp", "dcg0", "dcg", "momx", "momy", "cgmxx", "cgmxy", "cgmyy",
-        "ar", "oneovar", "oneovdx", "oneovdy", "dxn", "dxs", "dye", "dyw"}
+        "ar", "oneovar", "oneovdx", "oneovdy", "dxn", "dxs", "dye", "dyw",
+        "taux_ocntop", "tauy_ocntop", "taux_ocnbot", "tauy_ocnbot", "taux_snl", "tauy_snl", "epsx_ocn", "epsy_ocn",
+        "epsx_atm", "epsy_atm", "tailocnx", "tailocny", "taux1", "tauy1", "taux2", "tauy2", "taux3", "tauy3"}
 _IMM = {"wspd", "wdir", "uc", "vc", "rhoa", "rhow", "rhorat", "fice", "d", "dx", "dy"}
 _TABLES = {"k", "logl2overz", "fkovg", "k4", "k3dk", "kdk", "cothkd", "sbf", "sdv", "bf1_renorm", "bf2_renorm"}
 _SCALARS = {"dts", "dta", "dtr", "dtr_temp", "sumt", "dtamin", "cgmax", "dth"}
