@@ -144,6 +144,21 @@ int umwm_gpu_get_state_noalloc(float* F, float* ust);
  * Ensemble members use restart/umwmrst_<time>_m<member>.nc. */
 int umwm_gpu_write_restart(const char* path);
 
+/* output_grid_nc, umwm_io.F90:317-854: write the gridded output of the
+ * last outer step (one-member models) to a netCDF file in the reference's
+ * layout: dimensions x, y, f, th, time (record) and z with the Stokes
+ * drift; the reference's variables in its order (frequency, theta, lon,
+ * lat, seamask, depth, forcing, momentum, stresses with the stress('ocn')
+ * parts, tails, cd, ust, swh and the mean and dominant wave fields,
+ * physics_time_step), each with its description and units; land cells
+ * NaN.  Needs the stress('ocn') fields (option stress_ocn, or a run that
+ * wrote output).  umwm_gpu_run also writes output/umwmout_<time>.nc at
+ * the times the namelist's outgrid asks for when the directory output
+ * exists, computing stress('ocn') for those steps (umwm_top.F90:165-177);
+ * it writes nothing otherwise, as the reference's failed nf90_create
+ * does. */
+int umwm_gpu_write_output(const char* path);
+
 /* Copy a named field into out (n floats).  Names are the reference's
  * variable names: wet-point fields (ht, mwp, mwd, mss, mwl, dwd, dwl, dwp,
  * dcp0, dcp, dcg0, dcg, momx, momy, cgmxx, cgmxy, cgmyy, ustar, cd, taux,

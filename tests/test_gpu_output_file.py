@@ -1,0 +1,110 @@
+"""Gridded output in the reference's netCDF layout (umwm_io.F90:317-854).
+
+The files the library writes are read back with scipy's netCDF-3 reader, an
+implementation independent of the library's writer.  Each wet cell of a
+variable must equal the wet-point field read through the C ABI at that
+cell, land cells are NaN, and the variables come in the reference's order
+with its descriptions and units.
+"""
+import datetime
+import os
+import re
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# the reference's variable order (umwm_io.F90:360-633), without the Stokes drift
+VARIABLES = [
+    "frequency", "theta", "lon", "lat", "seamask", "depth", "wspd", "wdir", "uc", "vc", "rhoa", "rhow", "fice",
+    "psim", "momx", "momy", "cgmxx", "cgmxy", "cgmyy", "shelt", "epsx_atm", "epsy_atm", "epsx_ocn", "epsy_ocn",
+    "taux_form", "tauy_form", "taux_form_1", "tauy_form_1", "taux_form_2", "tauy_form_2", "taux_form_3",
+    "tauy_form_3", "taux_skin", "tauy_skin", "taux_diag", "tauy_diag", "taux_ocn", "tauy_ocn", "taux_bot",
+    "tauy_bot", "taux_snl", "tauy_snl", "tailatmx", "tailatmy", "tailocnx", "tailocny", "cd", "ust", "swh",
+    "mss", "mwp", "mwl", "mwd", "dwp", "dwl", "dwd", "dcp0", "dcg0", "dcp", "dcg", "physics_time_step"]
+
+# output variable -> wet-point field of the C ABI
+WET = {"swh": "ht", "ust": "ustar", "cd": "cd", "mss": "mss", "mwp": "mwp", "mwd": "mwd", "dwp": "dwp",
+       "momx": "momx", "cgmxy": "cgmxy", "taux_form": "taux_form", "taux_skin": "taux_skin",
+       "taux_ocn": "taux_ocntop", "tauy_bot": "tauy_ocnbot", "taux_snl": "taux_snl", "epsx_atm": "epsx_atm",
+       "epsy_ocn": "epsy_ocn", "taux_form_2": "taux2", "tailocnx": "tailocnx", "dcg": "dcg", "shelt": "shelt"}
+
+
+def _case():
+    from umwm_gb300 import configs
+
+    case = configs.hurricane(mm=40, nm=36, hours=2, dx=4000.0, dtg=600, seed=3)
+    nml = re.sub(r"outgrid\s*=\s*-?\d+", "outgrid = 1", case.nml)
+    assert "outgrid = 1" in nml
+    return case, nml
+
+
+def test_output_grid_files(lib_built, tmp_path, monkeypatch):
+    scipy_io = pytest.importorskip("scipy.io")
+    U = lib_built
+    monkeypatch.chdir(tmp_path)
+    os.makedirs("output")
+    case, nml = _case()
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=nml)
+    U.umwm_run(case.start, case.stop)
+    got = {v: U.get_field(w) for v, w in WET.items()}
+    mask = U.get_field_i("mask")  # (mm, nm)
+    d = U.dims()
+    freq, theta = U.get_field("f"), U.get_field("th")
+    U.write_output("explicit.nc")
+    U.umwm_finalize()
+
+    t0 = datetime.datetime.strptime(case.start, "%Y-%m-%d %H:%M:%S")
+    keys = [(t0 + datetime.timedelta(hours=h)).strftime("%Y-%m-%d_%H:%M:%S") for h in range(3)]
+    start_key, stop_key = keys[0], keys[-1]
+    assert stop_key == case.stop.replace(" ", "_")
+    # the start time (first substep) and each full hour of the 2-hour run
+    assert sorted(os.listdir("output")) == ["umwmout_%s.nc" % k for k in keys]
+
+    for path in ("output/umwmout_%s.nc" % stop_key, "explicit.nc"):
+        with scipy_io.netcdf_file(path, "r", mmap=False) as f:
+            assert f.dimensions["x"] == d["mm"] and f.dimensions["y"] == d["nm"]
+            assert f.dimensions["f"] == d["om"] and f.dimensions["th"] == d["pm"]
+            assert f.dimensions["time"] is None  # the record dimension
+            assert list(f.variables) == VARIABLES
+            assert f.variables["swh"].description == b"significant wave height"
+            assert f.variables["swh"].units == b"m"
+            assert f.variables["swh"].dimensions == ("time", "y", "x")
+            assert f.variables["seamask"].typecode() == "i"
+            sea = f.variables["seamask"][0]
+            np.testing.assert_array_equal(sea, mask.T)
+            wet = sea == 1
+            for v, ref in got.items():
+                a = f.variables[v][0]
+                assert a.shape == (d["nm"], d["mm"])
+                assert np.isnan(a[~wet]).all(), v
+                # wet points are numbered with x fastest, as C order reads them
+                np.testing.assert_array_equal(a[wet], ref, err_msg=v)
+            np.testing.assert_array_equal(f.variables["frequency"][:], freq)
+            np.testing.assert_array_equal(f.variables["theta"][:], theta)
+            assert np.isfinite(f.variables["depth"][0][wet]).all()
+
+    # the file written at the start time carries zero stress('ocn') fields
+    with scipy_io.netcdf_file("output/umwmout_%s.nc" % start_key, "r", mmap=False) as f:
+        sea = f.variables["seamask"][0] == 1
+        assert (f.variables["taux_ocn"][0][sea] == 0).all()
+        assert np.isfinite(f.variables["swh"][0][sea]).all()
+
+
+def test_output_grid_needs_directory(lib_built, tmp_path, monkeypatch):
+    """Without an output directory the run writes nothing and goes on, as
+    the reference's failed nf90_create does."""
+    U = lib_built
+    monkeypatch.chdir(tmp_path)
+    case, nml = _case()
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=nml)
+    U.umwm_run(case.start, case.stop)
+    ht = U.get_field("ht")
+    U.umwm_finalize()
+    assert not os.path.exists("output")
+    assert np.isfinite(ht).all()

@@ -14,7 +14,7 @@ EXPORTS = [
     "umwm_gpu_put_gridtopo", "umwm_gpu_put_exclude", "umwm_gpu_put_forcing", "umwm_gpu_put_restart",
     "umwm_gpu_clear_inputs", "umwm_gpu_initialize", "umwm_gpu_initialize_text", "umwm_gpu_run",
     "umwm_gpu_finalize", "umwm_gpu_setup_host", "umwm_gpu_get_dims", "umwm_gpu_get_state", "umwm_gpu_set_state",
-    "umwm_gpu_get_state_noalloc", "umwm_gpu_write_restart",
+    "umwm_gpu_get_state_noalloc", "umwm_gpu_write_restart", "umwm_gpu_write_output",
     "umwm_gpu_get_field", "umwm_gpu_get_field_i", "umwm_gpu_get_screen", "umwm_gpu_set_option",
     "umwm_gpu_get_stat", "umwm_gpu_last_error", "umwm_gpu_ensemble_add", "umwm_gpu_ensemble_initialize",
     "umwm_gpu_select_member", "umwm_gpu_surrogate_init", "umwm_gpu_surrogate_get_params",
@@ -64,6 +64,7 @@ def lib():
         "umwm_gpu_set_state": [fp, fp],
         "umwm_gpu_get_state_noalloc": [fp, fp],
         "umwm_gpu_write_restart": [c],
+        "umwm_gpu_write_output": [c],
         "umwm_gpu_get_field": [c, fp, ctypes.c_long],
         "umwm_gpu_get_field_i": [c, ip, ctypes.c_long],
         "umwm_gpu_get_screen": [dp, ctypes.c_long, ctypes.POINTER(ctypes.c_long)],

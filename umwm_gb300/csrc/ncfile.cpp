@@ -17,7 +17,7 @@ namespace nc {
 namespace {
 
 constexpr uint32_t TAG_DIM = 0x0A, TAG_VAR = 0x0B, TAG_ATT = 0x0C;
-constexpr uint32_t NC_CHAR = 2, NC_FLOAT = 5;
+constexpr uint32_t NC_CHAR = 2, NC_INT = 4, NC_FLOAT = 5;
 
 struct Buf {
   std::vector<unsigned char> b;
@@ -38,10 +38,15 @@ struct Buf {
   }
 };
 
-void put_be_floats(const float* in, size_t n, unsigned char* out) {
+void put_be_floats(const float* in, size_t n, unsigned char* out, bool as_int) {
   for (size_t i = 0; i < n; ++i) {
     uint32_t u;
-    std::memcpy(&u, &in[i], 4);
+    if (as_int) {
+      const int32_t v = (int32_t)in[i];
+      std::memcpy(&u, &v, 4);
+    } else {
+      std::memcpy(&u, &in[i], 4);
+    }
     out[4 * i] = (unsigned char)(u >> 24);
     out[4 * i + 1] = (unsigned char)(u >> 16);
     out[4 * i + 2] = (unsigned char)(u >> 8);
@@ -60,25 +65,44 @@ using File = std::unique_ptr<FILE, FileCloser>;
 
 bool write(const std::string& path, const std::vector<std::pair<std::string, size_t>>& dims,
            const std::vector<Var>& vars, std::string& err) {
-  std::vector<size_t> count(vars.size(), 1);
+  std::vector<size_t> count(vars.size(), 1);  // elements written (one record for record variables)
+  std::vector<bool> rec(vars.size(), false);
+  int nrecdims = 0;
+  for (auto& d : dims) {
+    if (d.second == 0) ++nrecdims;
+    if (d.second > 0xFFFFFFFFull) {
+      err = "netCDF write: dimension length out of range";
+      return false;
+    }
+  }
+  if (nrecdims > 1) {
+    err = "netCDF write: more than one record dimension";
+    return false;
+  }
   for (size_t v = 0; v < vars.size(); ++v)
-    for (int d : vars[v].dims) {
+    for (size_t a = 0; a < vars[v].dims.size(); ++a) {
+      const int d = vars[v].dims[a];
       if (d < 0 || d >= (int)dims.size()) {
         err = "netCDF write: bad dimension id";
         return false;
       }
-      count[v] *= dims[d].second;
+      if (dims[d].second == 0) {
+        if (a != 0) {
+          err = "netCDF write: the record dimension must come first";
+          return false;
+        }
+        rec[v] = true;
+      } else {
+        count[v] *= dims[d].second;
+      }
     }
-  for (auto& d : dims)
-    if (d.second == 0 || d.second > 0xFFFFFFFFull) {
-      err = "netCDF write: dimension length out of range";
-      return false;
-    }
+  bool any_rec = false;
+  for (bool r : rec) any_rec = any_rec || r;
   // header with every variable's begin offset; its size does not depend on them
   auto header = [&](const std::vector<uint64_t>& begin) {
     Buf h;
     h.bytes("CDF\x02", 4);
-    h.u32(0);  // no records
+    h.u32(any_rec ? 1u : 0u);  // records
     h.u32(TAG_DIM);
     h.u32((uint32_t)dims.size());
     for (auto& d : dims) {
@@ -107,22 +131,30 @@ bool write(const std::string& path, const std::vector<std::pair<std::string, siz
           h.bytes(a.second.data(), a.second.size());
         }
       }
-      h.u32(NC_FLOAT);
+      h.u32(x.is_int ? NC_INT : NC_FLOAT);
       const uint64_t vs = count[v] * 4;
       h.u32(vs > 0xFFFFFFFCull ? 0xFFFFFFFFu : (uint32_t)vs);  // too large: only legal for the last variable
       h.u64(begin[v]);
     }
     return h;
   };
-  for (size_t v = 0; v + 1 < vars.size(); ++v)
-    if (count[v] * 4 > 0xFFFFFFFCull) {
+  // data: the fixed-size variables in order, then the one record (each
+  // record variable's slab in order)
+  std::vector<size_t> order;
+  for (size_t v = 0; v < vars.size(); ++v)
+    if (!rec[v]) order.push_back(v);
+  for (size_t v = 0; v < vars.size(); ++v)
+    if (rec[v]) order.push_back(v);
+  // a variable of more than 4 GiB is only legal as the last fixed-size one of a file without records
+  for (size_t a = 0; a < order.size(); ++a)
+    if (count[order[a]] * 4 > 0xFFFFFFFCull && (any_rec || a + 1 != order.size())) {
       err = "netCDF write: only the last variable may exceed 4 GiB";
       return false;
     }
   std::vector<uint64_t> begin(vars.size(), 0);
   const size_t hsize = header(begin).b.size();
   uint64_t off = hsize;
-  for (size_t v = 0; v < vars.size(); ++v) {
+  for (size_t v : order) {
     begin[v] = off;
     off += (count[v] * 4 + 3) / 4 * 4;
   }
@@ -139,14 +171,14 @@ bool write(const std::string& path, const std::vector<std::pair<std::string, siz
   const size_t CH = 1 << 20;
   std::vector<float> vals(CH);
   std::vector<unsigned char> raw(CH * 4);
-  for (size_t v = 0; v < vars.size(); ++v) {
+  for (size_t v : order) {
     for (size_t first = 0; first < count[v]; first += CH) {
       const size_t n = std::min(CH, count[v] - first);
       if (!vars[v].fill(first, n, vals.data())) {
         err = "netCDF write: no data for variable " + vars[v].name;
         return false;
       }
-      put_be_floats(vals.data(), n, raw.data());
+      put_be_floats(vals.data(), n, raw.data(), vars[v].is_int);
       if (std::fwrite(raw.data(), 1, n * 4, f.get()) != n * 4) {
         err = "netCDF write: write failed on " + path;
         return false;

@@ -1,7 +1,9 @@
 // Minimal netCDF classic-format files (64-bit offset variant, "CDF\2"),
-// written and read without the netCDF library: the restart files of the
-// reference (restart/umwmrst_<time>.nc, umwm_restart.F90:19-154) in its own
-// layout.  Only what those files use: fixed-size dimensions, float
+// written and read without the netCDF library: the restart files
+// (restart/umwmrst_<time>.nc, umwm_restart.F90:19-154) and the gridded
+// output (output/umwmout_<time>.nc, umwm_io.F90:317-854) in the reference's
+// layouts.  Only what those files use: fixed-size dimensions and one record
+// (unlimited) dimension holding one record, float and 32-bit integer
 // variables, text attributes.  Values are stored big-endian as the format
 // requires; the host byte order does not matter.
 #pragma once
@@ -21,9 +23,12 @@ struct Var {
   std::vector<std::pair<std::string, std::string>> atts;  // text attributes
   // fills out[0..count) with elements [first, first+count) of the variable
   std::function<bool(size_t first, size_t count, float* out)> fill;
+  bool is_int = false;  // stored as 32-bit integers (the fill values are converted)
 };
 
-// Write a file with the given dimensions (name, length) and float variables.
+// Write a file with the given dimensions (name, length) and variables.  A
+// dimension of length 0 is the record (unlimited) dimension; it must be a
+// variable's first (slowest) dimension, and the file holds one record.
 bool write(const std::string& path, const std::vector<std::pair<std::string, size_t>>& dims,
            const std::vector<Var>& vars, std::string& err);
 

@@ -7,8 +7,10 @@
 // end the inner loop, or none at all when the loop runs as a CUDA graph
 // with a device-side while node.
 #include <cuda_runtime.h>
+#include <sys/stat.h>
 
 #include <algorithm>
+#include <functional>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -662,12 +664,191 @@ int restart_write(Model& M, int m, const std::string& path) {
   return UMWM_OK;
 }
 
+// output_grid_nc, umwm_io.F90:317-854: output/umwmout_<time>.nc with the
+// reference's dimensions (x, y, f, th, time as the record dimension, z with
+// the Stokes drift) and variables, in its order.  Wet-point fields go to
+// their (m, n) cell and land cells are NaN, as gatherfield leaves them
+// (umwm_io.F90:856-901); psim is 0 as in the reference (umwm_init.F90:341-342).
+int output_grid(Model& M, const std::string& path) {
+  const Params& p = M.prm;
+  const MemberHost& mh = M.mem[0];
+  const HostModel& H = mh.H;
+  const Ptrs& P = M.P;
+  const int N = mh.N, mm = H.mm, nm = H.nm;
+  const size_t n2 = (size_t)mm * nm;
+  CU(cudaStreamSynchronize(M.st));
+  const float nan = std::numeric_limits<float>::quiet_NaN();
+  // a wet-point field (device, wet points first) spread on the grid
+  auto spread = [&](const float* dev, std::vector<float>& out) -> bool {
+    std::vector<float> w(N);
+    if (cudaMemcpy(w.data(), dev, (size_t)N * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return false;
+    out.assign(n2, nan);
+    for (int i = 1; i <= N; ++i) out[H.i2(H.mi[i], H.ni[i])] = w[i - 1];
+    return true;
+  };
+  struct Field {
+    const char *name, *desc, *units;
+    std::function<bool(std::vector<float>&)> make;  // the whole variable
+    int kind;  // 0: (time, y, x), 1: (f), 2: (th), 3: (z), 4: (time, z, y, x)
+    bool is_int;
+  };
+  auto wet = [&](const float* dev) { return [&, dev](std::vector<float>& o) { return spread(dev + mh.off, o); }; };
+  auto allp = [&](const float* dev) { return [&, dev](std::vector<float>& o) { return spread(dev + mh.nmoff, o); }; };
+  auto ocn = [&](int q) {
+    return [&, q](std::vector<float>& o) { return spread(P.ocn + (size_t)q * p.ldN + mh.off, o); };
+  };
+  auto host2d = [&](const std::vector<float>& v) { return [&v](std::vector<float>& o) { o = v; return true; }; };
+  auto stokes = [&](const float* dev) {
+    return [&, dev](std::vector<float>& o) {
+      o.assign((size_t)H.lm * n2, nan);
+      std::vector<float> lev;
+      for (int l = 0; l < H.lm; ++l) {
+        if (!spread(dev + (size_t)l * p.ldN + mh.off, lev)) return false;
+        std::copy(lev.begin(), lev.end(), o.begin() + (size_t)l * n2);
+      }
+      return true;
+    };
+  };
+  std::vector<float> mask_f(H.mask.begin(), H.mask.end());
+  std::vector<float> depth_lm(H.depth.begin(), H.depth.end());
+  std::vector<Field> F;
+  if (H.stokes && H.lm > 0) {
+    F.push_back({"z", "depth", "m", host2d(depth_lm), 3, false});
+    F.push_back({"u_stokes", "stokes drift x-component", "m/s", stokes(P.us), 4, false});
+    F.push_back({"v_stokes", "stokes drift y-component", "m/s", stokes(P.vs), 4, false});
+    F.push_back({"d_stokes", "stokes drift e-folding depth", "m", wet(P.ds), 0, false});
+  }
+  F.push_back({"frequency", "frequency", "hz", host2d(H.f), 1, false});
+  F.push_back({"theta", "directions", "rad", host2d(H.th), 2, false});
+  F.push_back({"lon", "longitude", "degrees east", host2d(H.lon), 0, false});
+  F.push_back({"lat", "latitude", "degrees north", host2d(H.lat), 0, false});
+  F.push_back({"seamask", "seamask", "non-dimensional", host2d(mask_f), 0, true});
+  F.push_back({"depth", "ocean depth", "m", host2d(H.d_2d), 0, false});
+  F.push_back({"wspd", "wind speed", "m/s", allp(P.wspd), 0, false});
+  F.push_back({"wdir", "wind direction", "rad", allp(P.wdir), 0, false});
+  F.push_back({"uc", "ocean current, x-component", "m/s", allp(P.uc), 0, false});
+  F.push_back({"vc", "ocean current, y-component", "m/s", allp(P.vc), 0, false});
+  F.push_back({"rhoa", "air density", "kg/m^3", allp(P.rhoa), 0, false});
+  F.push_back({"rhow", "water density", "kg/m^3", allp(P.rhow), 0, false});
+  F.push_back({"fice", "seaice fraction", "non-dimensional", allp(P.fice), 0, false});
+  F.push_back({"psim", "universal stability function for momentum", "non-dimensional",
+               [&](std::vector<float>& o) {
+                 o.assign(n2, nan);
+                 for (int i = 1; i <= N; ++i) o[H.i2(H.mi[i], H.ni[i])] = 0.f;
+                 return true;
+               }, 0, false});
+  F.push_back({"momx", "momentum, x-component", "kgm/s", wet(P.momx), 0, false});
+  F.push_back({"momy", "momentum, y-component", "kgm/s", wet(P.momy), 0, false});
+  F.push_back({"cgmxx", "cg*momentum, xx-component", "kgm^2/s^2", wet(P.cgmxx), 0, false});
+  F.push_back({"cgmxy", "cg*momentum, xy-component", "kgm^2/s^2", wet(P.cgmxy), 0, false});
+  F.push_back({"cgmyy", "cg*momentum, yy-component", "kgm^2/s^2", wet(P.cgmyy), 0, false});
+  F.push_back({"shelt", "sheltering coefficient", "non-dimensional", wet(P.shelt), 0, false});
+  F.push_back({"epsx_atm", "wave energy growth flux, x-component", "kg/s^3", ocn(OCN_EPSX_ATM), 0, false});
+  F.push_back({"epsy_atm", "wave energy growth flux, y-component", "kg/s^3", ocn(OCN_EPSY_ATM), 0, false});
+  F.push_back({"epsx_ocn", "wave energy dissipation flux, x-component", "kg/s^3", ocn(OCN_EPSX_OCN), 0, false});
+  F.push_back({"epsy_ocn", "wave energy dissipation flux, y-component", "kg/s^3", ocn(OCN_EPSY_OCN), 0, false});
+  F.push_back({"taux_form", "form drag, x-component", "n/m^2", wet(P.taux_form), 0, false});
+  F.push_back({"tauy_form", "form drag, y-component", "n/m^2", wet(P.tauy_form), 0, false});
+  F.push_back({"taux_form_1", "form drag, part 1, x-component", "n/m^2", ocn(OCN_TAUX1), 0, false});
+  F.push_back({"tauy_form_1", "form drag, part 1, y-component", "n/m^2", ocn(OCN_TAUY1), 0, false});
+  F.push_back({"taux_form_2", "form drag, part 2, x-component", "n/m^2", ocn(OCN_TAUX2), 0, false});
+  F.push_back({"tauy_form_2", "form drag, part 2, y-component", "n/m^2", ocn(OCN_TAUY2), 0, false});
+  F.push_back({"taux_form_3", "form drag, part 3, x-component", "n/m^2", ocn(OCN_TAUX3), 0, false});
+  F.push_back({"tauy_form_3", "form drag, part 3, y-component", "n/m^2", ocn(OCN_TAUY3), 0, false});
+  F.push_back({"taux_skin", "skin drag, x-component", "n/m^2", wet(P.taux_skin), 0, false});
+  F.push_back({"tauy_skin", "skin drag, y-component", "n/m^2", wet(P.tauy_skin), 0, false});
+  F.push_back({"taux_diag", "diagnostic form drag, x-component", "n/m^2", wet(P.taux_diag), 0, false});
+  F.push_back({"tauy_diag", "diagnostic form drag, y-component", "n/m^2", wet(P.tauy_diag), 0, false});
+  F.push_back({"taux_ocn", "momentum flux from breaking waves to ocean top, x-component", "n/m^2",
+               ocn(OCN_TAUX_TOP), 0, false});
+  F.push_back({"tauy_ocn", "momentum flux from breaking waves to ocean top, y-component", "n/m^2",
+               ocn(OCN_TAUY_TOP), 0, false});
+  F.push_back({"taux_bot", "momentum flux from waves to ocean bottom, x-component", "n/m^2", ocn(OCN_TAUX_BOT), 0,
+               false});
+  F.push_back({"tauy_bot", "momentum flux from waves to ocean bottom, y-component", "n/m^2", ocn(OCN_TAUY_BOT), 0,
+               false});
+  F.push_back({"taux_snl", "momentum flux due to snl, x-component", "n/m^2", ocn(OCN_TAUX_SNL), 0, false});
+  F.push_back({"tauy_snl", "momentum flux due to snl, y-component", "n/m^2", ocn(OCN_TAUY_SNL), 0, false});
+  F.push_back({"tailatmx", "atmosphere tail stress part, x-component", "n/m^2", wet(P.tailatmx), 0, false});
+  F.push_back({"tailatmy", "atmosphere tail stress part, y-component", "n/m^2", wet(P.tailatmy), 0, false});
+  F.push_back({"tailocnx", "ocean tail stress part, x-component", "n/m^2", ocn(OCN_TAILX), 0, false});
+  F.push_back({"tailocny", "ocean tail stress part, y-component", "n/m^2", ocn(OCN_TAILY), 0, false});
+  F.push_back({"cd", "drag coefficient of air", "non-dimensional", wet(P.cd), 0, false});
+  F.push_back({"ust", "friction velocity of air", "m/s", wet(P.ustar), 0, false});
+  F.push_back({"swh", "significant wave height", "m", wet(P.ht), 0, false});
+  F.push_back({"mss", "mean-squared slope", "non-dimensional", wet(P.mss), 0, false});
+  F.push_back({"mwp", "mean wave period", "s", wet(P.mwp), 0, false});
+  F.push_back({"mwl", "mean wavelength", "m", wet(P.mwl), 0, false});
+  F.push_back({"mwd", "mean wave direction", "rad", wet(P.mwd), 0, false});
+  F.push_back({"dwp", "dominant wave period", "s", wet(P.dwp), 0, false});
+  F.push_back({"dwl", "dominant wavelength", "m", wet(P.dwl), 0, false});
+  F.push_back({"dwd", "dominant wave direction", "rad", wet(P.dwd), 0, false});
+  F.push_back({"dcp0", "dominant phase speed, intrinsic", "m/s", wet(P.dcp0), 0, false});
+  F.push_back({"dcg0", "dominant group speed, intrinsic", "m/s", wet(P.dcg0), 0, false});
+  F.push_back({"dcp", "dominant phase speed", "m/s", wet(P.dcp), 0, false});
+  F.push_back({"dcg", "dominant group speed", "m/s", wet(P.dcg), 0, false});
+  F.push_back({"physics_time_step", "Physics time step", "s", wet(P.phys), 0, false});
+
+  std::vector<std::pair<std::string, size_t>> dims = {
+      {"x", (size_t)mm}, {"y", (size_t)nm}, {"f", (size_t)p.O}, {"th", (size_t)p.P}, {"time", 0}};
+  const int X = 0, Y = 1, FD = 2, TH = 3, T = 4;
+  if (H.stokes && H.lm > 0) dims.push_back({"z", (size_t)H.lm});
+  const int Z = 5;
+  std::vector<nc::Var> vars;
+  std::vector<std::vector<float>> cache(F.size());
+  bool ok = true;
+  for (size_t q = 0; q < F.size(); ++q) {
+    nc::Var v;
+    v.name = F[q].name;
+    v.atts = {{"description", F[q].desc}, {"units", F[q].units}};
+    v.is_int = F[q].is_int;
+    switch (F[q].kind) {
+      case 1: v.dims = {FD}; break;
+      case 2: v.dims = {TH}; break;
+      case 3: v.dims = {Z}; break;
+      case 4: v.dims = {T, Z, Y, X}; break;
+      default: v.dims = {T, Y, X}; break;
+    }
+    v.fill = [&, q](size_t first, size_t n, float* out) {
+      if (first == 0 && !F[q].make(cache[q])) {
+        ok = false;
+        return false;
+      }
+      if (first + n > cache[q].size()) return false;
+      std::memcpy(out, cache[q].data() + first, n * 4);
+      if (first + n == cache[q].size()) std::vector<float>().swap(cache[q]);
+      return true;
+    };
+    vars.push_back(std::move(v));
+  }
+  std::string err;
+  if (!nc::write(path, dims, vars, err)) return fail(ok ? UMWM_ERR_INPUT : UMWM_ERR_CUDA, "output_grid_nc: " + err);
+  return UMWM_OK;
+}
+
+// output/umwmout_<time>.nc; a file that cannot be written is reported and
+// the run goes on, as the reference ignores the netCDF status there
+void write_output_file(Model& M, int64_t t) {
+  const std::string path = "output/umwmout_" + time_to_string(t, '_') + ".nc";
+  if (output_grid(M, path) != UMWM_OK) {
+    std::fprintf(stderr, "umwm: output_grid_nc: %s not written (%s)\n", path.c_str(), g_err.c_str());
+    g_err.clear();
+  } else if (M.verbose) {
+    std::printf("umwm: output_grid_nc: written to %s\n", path.c_str());
+  }
+}
+
 int check_ctl(Model& M) {
   std::vector<Ctl> c(M.mem.size());
   CU(cudaMemcpy(c.data(), M.mem[0].ctl, c.size() * sizeof(Ctl), cudaMemcpyDeviceToHost));
   for (auto& x : c)
     if (x.err) return fail(UMWM_ERR_TIMEOUT, "a device-side wait gave up");
   return UMWM_OK;
+}
+
+bool dir_exists(const char* path) {
+  struct stat st;
+  return ::stat(path, &st) == 0 && S_ISDIR(st.st_mode);
 }
 
 // Buffers of stress('ocn'): the last substep's source terms and the outputs.
@@ -817,6 +998,10 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     if ((rc = member_substeps(M, sub))) return rc;
     for (size_t m = 0; m < M.mem.size(); ++m) M.mem[m].substep_mark = sub[m];
   }
+  // the first substep of a model also writes output/umwmout_<start>.nc
+  // (umwm_top.F90:121-127), without stress('ocn'): its fields are zero
+  bool first_out = M.first && M.mem[0].H.outgrid > 0 && M.mem.size() == 1 && dir_exists("output");
+  if (first_out && (rc = ensure_ocn(M))) return rc;
   CU(cudaEventRecord(M.ev0, M.st));
   int64_t now = t0;
   while (now < t1) {
@@ -830,7 +1015,11 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     const HostModel& H0 = M.mem[0].H;
     const int64_t sod = now % 86400;
     const bool grid_due = (H0.outgrid > 0 && (sod / 3600) % H0.outgrid == 0 && sod % 3600 == 0) || H0.outgrid == -1;
-    const bool ocn_due = M.ocn_every || (grid_due && M.P.src_sin);
+    // gridded output goes to output/umwmout_<time>.nc when that directory
+    // exists (the reference's nf90_create fails there silently otherwise);
+    // ensembles write none
+    const bool grid_write = grid_due && M.mem.size() == 1 && dir_exists("output");
+    const bool ocn_due = M.ocn_every || grid_write;
     if (ocn_due) {
       if ((rc = ensure_ocn(M))) return rc;
       static const int one = 1;
@@ -856,6 +1045,10 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
       }
       if ((rc = substep(M))) return rc;
       ++inner;
+      if (first_out) {
+        first_out = false;
+        write_output_file(M, t0);
+      }
       CU(cudaMemcpyAsync(M.flag_h, M.d_glob, sizeof(Global), cudaMemcpyDeviceToHost, M.st));
       CU(cudaStreamSynchronize(M.st));
       collect_timings(M);
@@ -873,6 +1066,7 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
       CU(cudaMemcpyAsync(&M.d_glob->save_src, &zero, sizeof(int), cudaMemcpyHostToDevice, M.st));
       M.launches++;
     }
+    if (grid_write) write_output_file(M, now);
     if (M.verbose) print_screen(M);
     // restart output, umwm_top.F90:183-190 (with the reference's test of
     // outspec == -1 for writing every step)
@@ -1169,6 +1363,15 @@ int umwm_gpu_get_state(float* F, float* ust) {
   return UMWM_OK;
 }
 
+int umwm_gpu_write_output(const char* path) {
+  Model* M = need_model(true);
+  if (!M) return UMWM_ERR_STATE;
+  if (!path) return fail(UMWM_ERR_ARG, "write_output: null path");
+  if (M->mem.size() != 1) return fail(UMWM_ERR_UNSUPPORTED, "write_output: one-member models only");
+  if (!M->P.ocn) return fail(UMWM_ERR_STATE, "write_output: stress('ocn') has not run (option stress_ocn)");
+  return output_grid(*M, path);
+}
+
 int umwm_gpu_write_restart(const char* path) {
   Model* M = need_model(true);
   if (!M) return UMWM_ERR_STATE;
@@ -1263,6 +1466,22 @@ int umwm_gpu_get_field(const char* name, float* out, long n) {
     out[0] = v;
     return UMWM_OK;
   };
+  // source terms the last stress('ocn') step kept (its last substep's Sin,
+  // Sds after cothkd and Snl), in the reference's (i, th, f) layout
+  if (s == "ssin" || s == "sds" || s == "snl") {
+    if (!M->P.src_sin) return fail(UMWM_ERR_STATE, "get_field: " + s + " is kept by stress('ocn') steps only");
+    const size_t cnt = (size_t)M->prm.O * M->prm.P * mh.N;
+    if (need((long)cnt)) return UMWM_ERR_ARG;
+    const float* src = s == "ssin" ? M->P.src_sin : s == "sds" ? M->P.src_sds : M->P.src_snl;
+    float* tmp = nullptr;
+    CU(cudaMalloc(&tmp, cnt * 4));
+    cudaError_t e = launch_to_ref(M->prm, src, tmp, mh.off, mh.N, M->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(M->st);
+    if (e == cudaSuccess) e = cudaMemcpy(out, tmp, cnt * 4, cudaMemcpyDeviceToHost);
+    cudaFree(tmp);
+    CU(e);
+    return UMWM_OK;
+  }
   if (s == "ar") return wet_host(H.ar);
   if (s == "oneovar") return wet_host(H.oneovar);
   if (s == "oneovdx") return wet_host(H.oneovdx);

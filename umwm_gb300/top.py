@@ -138,6 +138,8 @@ def get_field(name):
         shape = (im, om)
     elif name in ("cp0", "cg0"):
         shape = (im + 1, om)
+    elif name in ("ssin", "sds", "snl"):
+        shape = (im, pm, om)  # the source terms a stress('ocn') step kept
     elif name in ("us", "vs"):
         shape = (lm, im)
     elif name == "f":
@@ -200,6 +202,12 @@ def get_state_noalloc():
 def write_restart(path):
     """restart_write: the selected member's state as a netCDF restart file."""
     check(lib().umwm_gpu_write_restart(str(path).encode()))
+
+
+def write_output(path):
+    """output_grid_nc: the gridded output of the last outer step as a netCDF
+    file (needs set_option("stress_ocn", 1) before the run)."""
+    check(lib().umwm_gpu_write_output(str(path).encode()))
 
 
 def set_state(F=None, ust=None):
