@@ -15,7 +15,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-# the reference's variable order (umwm_io.F90:360-633), without the Stokes drift
+# the reference's variable order after the Stokes drift (umwm_io.F90:360-633)
 VARIABLES = [
     "frequency", "theta", "lon", "lat", "seamask", "depth", "wspd", "wdir", "uc", "vc", "rhoa", "rhow", "fice",
     "psim", "momx", "momy", "cgmxx", "cgmxy", "cgmyy", "shelt", "epsx_atm", "epsy_atm", "epsx_ocn", "epsy_ocn",
@@ -52,8 +52,10 @@ def test_output_grid_files(lib_built, tmp_path, monkeypatch):
     U.umwm_run(case.start, case.stop)
     got = {v: U.get_field(w) for v, w in WET.items()}
     mask = U.get_field_i("mask")  # (mm, nm)
+    ii = U.get_field_i("ii").T  # point number (1-based) of each cell, 0 on land, (nm, mm)
     d = U.dims()
     freq, theta = U.get_field("f"), U.get_field("th")
+    stokes_u = U.get_field("us")  # (lm, im)
     U.write_output("explicit.nc")
     U.umwm_finalize()
 
@@ -69,20 +71,27 @@ def test_output_grid_files(lib_built, tmp_path, monkeypatch):
             assert f.dimensions["x"] == d["mm"] and f.dimensions["y"] == d["nm"]
             assert f.dimensions["f"] == d["om"] and f.dimensions["th"] == d["pm"]
             assert f.dimensions["time"] is None  # the record dimension
-            assert list(f.variables) == VARIABLES
+            sea = f.variables["seamask"][0]
+            np.testing.assert_array_equal(sea, mask.T)
+            wet = sea == 1
+            # wet points are 1..im; boundary cells im+1..imm are not written
+            np.testing.assert_array_equal(wet, (ii > 0) & (ii <= d["im"]))
+            # the hurricane case has the Stokes drift on: z and its fields first
+            assert f.dimensions["z"] == d["lm"] > 0
+            assert list(f.variables) == ["z", "u_stokes", "v_stokes", "d_stokes"] + VARIABLES
+            assert f.variables["u_stokes"].dimensions == ("time", "z", "y", "x")
+            us = f.variables["u_stokes"][0]
+            for lev in range(d["lm"]):
+                np.testing.assert_array_equal(us[lev][wet], stokes_u[lev][ii[wet] - 1])
             assert f.variables["swh"].description == b"significant wave height"
             assert f.variables["swh"].units == b"m"
             assert f.variables["swh"].dimensions == ("time", "y", "x")
             assert f.variables["seamask"].typecode() == "i"
-            sea = f.variables["seamask"][0]
-            np.testing.assert_array_equal(sea, mask.T)
-            wet = sea == 1
             for v, ref in got.items():
                 a = f.variables[v][0]
                 assert a.shape == (d["nm"], d["mm"])
                 assert np.isnan(a[~wet]).all(), v
-                # wet points are numbered with x fastest, as C order reads them
-                np.testing.assert_array_equal(a[wet], ref, err_msg=v)
+                np.testing.assert_array_equal(a[wet], ref[ii[wet] - 1], err_msg=v)
             np.testing.assert_array_equal(f.variables["frequency"][:], freq)
             np.testing.assert_array_equal(f.variables["theta"][:], theta)
             assert np.isfinite(f.variables["depth"][0][wet]).all()
