@@ -173,7 +173,9 @@ int umwm_gpu_write_output(const char* path);
  * once it has run (option "stress_ocn", or an outer step with gridded
  * output due): taux_ocntop, tauy_ocntop, taux_ocnbot, tauy_ocnbot, taux_snl,
  * tauy_snl, epsx_ocn, epsy_ocn, epsx_atm, epsy_atm, tailocnx, tailocny,
- * taux1, tauy1, taux2, tauy2, taux3, tauy3. */
+ * taux1, tauy1, taux2, tauy2, taux3, tauy3; and the source terms its last
+ * substep kept, in get_state's (om, pm, im) layout: ssin, sds (after the
+ * cothkd factor) and snl (umwm_source_functions.F90:16-183). */
 int umwm_gpu_get_field(const char* name, float* out, long n);
 
 /* Integer fields: mask, ii (mm*nm); mi, ni, iw, ie, is, in, iiw, iie,
