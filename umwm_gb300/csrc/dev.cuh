@@ -61,11 +61,17 @@ struct Params {
   float g, explim, sin_fac, fieldscale1, fieldscale2, twopisds_fac, sds_power, inv_sds_power, mss_fac, snl_fac,
       sdt_fac, z, nu_air, kappa, fprog, dth, dthg, oneovdth, dtg, fice_lth, fice_uth, eulerinv, rhow0;
   float bf1, bf2;  // downshifting weights (umwm_init.F90:1290-1294)
+  // Sin factors of negative x (sin_fold): sin_fac fieldscale1, and with
+  // fieldscale2 where cos(wdir - th) > 0 (umwm_source_functions.F90:60-67)
+  float sin_neg1, sin_neg2;
   int winds, currents, air_density, water_density, seaice, restart, curvilinear, isglobal;
   int ice_possible;  // fice can exceed fice_lth somewhere
   int groups4;       // spectral kernels use 4 quarter-turn direction groups (option "direction_groups")
   float f[MAX_OM], dom[MAX_OM];
   float th[MAX_PM], cth[MAX_PM], sth[MAX_PM], c2th[MAX_PM], s2th[MAX_PM];
+  // max(cos th, 0), min(cos th, 0), max(sin th, 0), min(sin th, 0): the
+  // upwind weights of propagation (umwm_advection.F90:34-47)
+  float cthp[MAX_PM], cthm[MAX_PM], sthp[MAX_PM], sthm[MAX_PM];
   float depth[MAX_LM];
 };
 

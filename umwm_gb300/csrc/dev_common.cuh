@@ -35,7 +35,7 @@ __device__ __forceinline__ float shelter_coare35(float w) {
 // Per-point inputs of the wind-input source term, sin_d12
 // (umwm_source_functions.F90:16-82).
 struct WindIn {
-  float wspd, uc, vc, ustar25, shelt_sf, c1;
+  float wspd, uc, vc, ustar25, shelt_sf, shelt, c1;
   int oc;  // 1-based cut-off index; 0-based level o is prognostic when o < oc
 };
 
@@ -46,7 +46,8 @@ __device__ __forceinline__ WindIn load_wind(const Params& prm, const Ptrs& P, in
   w.uc = P.uc[ja];
   w.vc = P.vc[ja];
   w.ustar25 = 2.5f * ustar;
-  w.shelt_sf = P.shelt[jj] / prm.sin_fac;
+  w.shelt = P.shelt[jj];
+  w.shelt_sf = w.shelt / prm.sin_fac;
   // (1 - fice) * twopi * rhorat
   w.c1 = ((1.f - P.fice[ja]) * (2.f * 3.14159274f)) * P.rhorat[ja];
   w.oc = P.oc[jj];
@@ -65,6 +66,23 @@ __device__ __forceinline__ float sin_bin(const Params& prm, const WindIn& w, flo
   if (s < 0.f) s = s * prm.fieldscale1;
   if (s < 0.f && cw > 0.f) s = s * prm.fieldscale2;
   s = (w.c1 * s) * fkovg;
+  if (tail) s = fmaxf(s, 0.f);
+  return s;
+}
+
+// Sin of one bin from x = U cos(wdir - th) - cp0 - uc cos th - vc sin th,
+// umwm_source_functions.F90:39-80, with its factors folded: the reference
+// forms sin_fac |x| x, then multiplies by shelt/sin_fac where positive, by
+// fieldscale1 where negative and by fieldscale2 where still negative and
+// cos(wdir - th) > 0, then by (1 - fice) 2 pi rhorat and fkovg.  Here
+// (x |x|) is multiplied once by the factor its sign selects (shelt, or
+// sin_fac fieldscale1 [fieldscale2], prm.sin_neg1/2) and once by
+// gl = (1 - fice) 2 pi rhorat fkovg of the level: the same product in
+// another order (a few ulp apart), in fewer instructions.
+__device__ __forceinline__ float sin_fold(const Params& prm, float shelt, float x, float cw, float gl, bool tail) {
+  const float a = x * fabsf(x);
+  const float f = x > 0.f ? shelt : (cw > 0.f ? prm.sin_neg2 : prm.sin_neg1);
+  float s = (a * f) * gl;
   if (tail) s = fmaxf(s, 0.f);
   return s;
 }

@@ -10,7 +10,10 @@
 // (cge + |cge|) = 2 (cg0_i + cg0_ie) max(c, 0) and (cge - |cge|) uses min(c, 0):
 // the eight upwind terms of umwm_advection.F90:40-47 (and the current terms
 // of :76-82) collapse to five coefficients times E* at the point and its four
-// unrolled neighbours.  The east/west neighbours sit about one wet column
+// unrolled neighbours.  The half-turned group reads its neighbours in swapped
+// slots (east for west, north for south), so the upwind weights of every
+// group are the base group's compile-time max/min(cos th0, 0) and
+// max/min(sin th0, 0).  The east/west neighbours sit about one wet column
 // (~nm points) away and are served from L2, which holds the window of blocks
 // the CTAs in flight work on.
 // Refraction needs E* at p-1 and p+1: inside a group they are registers, at
@@ -34,16 +37,7 @@ __device__ __forceinline__ void bulk_prefetch(const void* p, unsigned bytes) {
 // Sin at one direction (same expression as the source kernels)
 __device__ __forceinline__ float sin_dir(const Params& prm, const WindIn& w, float U, float cw, float ucs, float vss,
                                          float cp0, float fkovg, bool tail) {
-  float s = U * cw - cp0 - ucs - vss;
-  s = (prm.sin_fac * fabsf(s)) * s;
-  if (s > 0.f) s = s * w.shelt_sf;
-  if (s < 0.f) {
-    s = s * prm.fieldscale1;
-    if (s < 0.f && cw > 0.f) s = s * prm.fieldscale2;
-  }
-  s = (w.c1 * s) * fkovg;
-  if (tail) s = fmaxf(s, 0.f);
-  return s;
+  return sin_fold(prm, w.shelt, U * cw - cp0 - ucs - vss, cw, w.c1 * fkovg, tail);
 }
 
 #ifndef UMWM_ADVECT_MINB
@@ -101,6 +95,17 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(c
     F0 = feup - fwdn + fnup - fsdn;
   }
   const float bx = (vce - vcw), by = (ucn - ucs);
+  // SW: the half-turned group (G = 2, q = 1) reads its east/west and
+  // north/south neighbours swapped, so that both groups use the base
+  // group's upwind weights max/min(cos th0, 0), max/min(sin th0, 0): with
+  // cos th = -cos th0 the east-west flux
+  //   DE (max(c,0) e0 + min(c,0) ee) - DW (max(c,0) ew + min(c,0) e0)
+  // equals the base-direction expression with (DE, ee) and (DW, ew) swapped
+  // (the same for north-south), and the current terms swap with them
+  constexpr bool SW = G == 2 && !CURV;
+  const bool flip = SW && q == 1;
+  const float cA = flip ? -fwup : fedn, cB = flip ? fedn : -fwup;
+  const float cNA = flip ? -fsup : fndn, cSB = flip ? fndn : -fsup;
 
 #pragma unroll
   for (int k = 0; k < H; ++k) {
@@ -119,6 +124,8 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(c
   const size_t hoff = (size_t)(q * H) * 32;
   const size_t oS = sidx(prm, 0, 0, jj) + hoff, oE = sidx(prm, 0, 0, ie) + hoff, oW = sidx(prm, 0, 0, iw) + hoff,
                oN = sidx(prm, 0, 0, in) + hoff, oSs = sidx(prm, 0, 0, is) + hoff;
+  // the swapped neighbour slots (SW): A/B east-west, NA/SB north-south
+  const size_t oA = flip ? oW : oE, oB = flip ? oE : oW, oNA = flip ? oSs : oN, oSB = flip ? oN : oSs;
   // stress_vector_integral divides by cp0 of the previous unrolled point
   // (assumed-shape dummy with lower bound 1 over cp0(:,0:im)),
   // umwm_stress.F90:401, :495-513; the member's first point uses its ghost
@@ -126,6 +133,8 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(c
   const size_t tS = tidx(prm, 0, 0, jj), tE = tidx(prm, 0, 0, ie), tW = tidx(prm, 0, 0, iw),
                tN = tidx(prm, 0, 0, in), tSs = tidx(prm, 0, 0, is), tP = tidx(prm, 0, 0, jprev);
   const float dtaq = 0.25f * dta * oneovar;
+  const float dtrq = dtr * prm.oneovdth;
+  const float dyA = flip ? dyw : dye, dyB = flip ? dye : dyw, dxNA = flip ? dxs : dxn, dxSB = flip ? dxn : dxs;
 
   float sx = 0.f, sy = 0.f, dsx = 0.f, dsy = 0.f, txom = 0.f, tyom = 0.f;
   // E* and ef of this block two frequencies ahead go to L2 in the background
@@ -160,12 +169,29 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(c
       const float esp = __shfl_sync(pm, es[0], (lane + PW) & 31);      // E* at p+1 for k = H-1 (group q+1)
       // ---- propagation, umwm_advection.F90:30-97
       const float cgi = __ldg(T + tS + T_CG0 * 32);
-      const float DE = 2.f * (cgi + __ldg(T + tE + T_CG0 * 32)) * dye;
-      const float DW = 2.f * (cgi + __ldg(T + tW + T_CG0 * 32)) * dyw;
-      const float DN = 2.f * (cgi + __ldg(T + tN + T_CG0 * 32)) * dxn;
-      const float DS = 2.f * (cgi + __ldg(T + tSs + T_CG0 * 32)) * dxs;
+      if (SW) {
+        const float DA = 2.f * (cgi + __ldg(T + (flip ? tW : tE) + T_CG0 * 32)) * dyA;
+        const float DB = 2.f * (cgi + __ldg(T + (flip ? tE : tW) + T_CG0 * 32)) * dyB;
+        const float DNA = 2.f * (cgi + __ldg(T + (flip ? tSs : tN) + T_CG0 * 32)) * dxNA;
+        const float DSB = 2.f * (cgi + __ldg(T + (flip ? tN : tSs) + T_CG0 * 32)) * dxSB;
 #pragma unroll
-      for (int k = 0; k < H; ++k) {
+        for (int k = 0; k < H; ++k) {
+          const float e0 = es[k];
+          const float ea = __ldg(ESo + oA + k * 32), eb = __ldg(ESo + oB + k * 32);
+          const float ena = __ldg(ESo + oNA + k * 32), esb = __ldg(ESo + oSB + k * 32);
+          const float cp = prm.cthp[k], cm = prm.cthm[k], sp = prm.sthp[k], sm = prm.sthm[k];
+          float flux = DA * (cp * e0 + cm * ea) - DB * (cp * eb + cm * e0) + DNA * (sp * e0 + sm * ena) -
+                       DSB * (sp * esb + sm * e0);
+          if (!zerocur) flux += F0 * e0 + cA * ea + cB * eb + cNA * ena + cSB * esb;
+          ef[k] = ef[k] - dtaq * flux;
+        }
+      }
+      const float DE = SW ? 0.f : 2.f * (cgi + __ldg(T + tE + T_CG0 * 32)) * dye;
+      const float DW = SW ? 0.f : 2.f * (cgi + __ldg(T + tW + T_CG0 * 32)) * dyw;
+      const float DN = SW ? 0.f : 2.f * (cgi + __ldg(T + tN + T_CG0 * 32)) * dxn;
+      const float DS = SW ? 0.f : 2.f * (cgi + __ldg(T + tSs + T_CG0 * 32)) * dxs;
+#pragma unroll
+      for (int k = 0; k < (SW ? 0 : H); ++k) {
         const float e0 = es[k];
         const float ee = __ldg(ESo + oE + k * 32), ew = __ldg(ESo + oW + k * 32);
         const float en = __ldg(ESo + oN + k * 32), esn = __ldg(ESo + oSs + k * 32);
@@ -177,38 +203,48 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(c
         float flux = DE * (cp * e0 + cm * ee) - DW * (cp * ew + cm * e0) + DN * (sp * e0 + sm * en) -
                      DS * (sp * esn + sm * e0);
         if (!zerocur) flux += F0 * e0 + fedn * ee - fwup * ew + fndn * en - fsup * esn;
-        ef[k] = ice ? 0.f : ef[k] - dtaq * flux;
+        ef[k] = ef[k] - dtaq * flux;
       }
       // ---- refraction, umwm_advection.F90:122-178
       if (o < ocr) {
         const float gx = 0.5f * (__ldg(T + tE + T_CP0 * 32) - __ldg(T + tW + T_CP0 * 32));
         const float gy = 0.5f * (__ldg(T + tN + T_CP0 * 32) - __ldg(T + tSs + T_CP0 * 32));
         const float hbx = 0.5f * bx, hby = 0.5f * by;
-        // rotation rate at base direction k of a group turned by (ca, cb):
-        // sin th = cb cos th0 + ca sin th0, cos th = ca cos th0 - cb sin th0
-        auto rot = [&](int k, float ca, float cb) {
-          if (G == 2) return (gx * ca * prm.sth[k] + hbx) * odx - (gy * ca * prm.cth[k] + hby) * ody;
-          return (gx * (cb * prm.cth[k] + ca * prm.sth[k]) + hbx) * odx -
-                 (gy * (ca * prm.cth[k] - cb * prm.sth[k]) + hby) * ody;
+        // rotation rate at base direction k of a group turned by (ca, cb)
+        // (sin th = cb cos th0 + ca sin th0, cos th = ca cos th0 - cb sin th0):
+        //   (gx sin th + hbx) odx - (gy cos th + hby) ody
+        //   = al sin th0 + be cos th0 + c0, the coefficients per group
+        const float c0 = hbx * odx - hby * ody;
+        auto coef = [&](float ca, float cb, float& al, float& be) {
+          al = gx * ca * odx + gy * cb * ody;
+          be = gx * cb * odx - gy * ca * ody;
         };
+        float alc, bec, alp, bep, aln, ben;
+        coef(ra, rb, alc, bec);
         // the previous group is this one turned back by 2pi/G, the next one turned on
-        const float pa = G == 2 ? -ra : rb, pb = G == 2 ? 0.f : -ra;
-        const float na = G == 2 ? -ra : -rb, nb = G == 2 ? 0.f : ra;
-        float rprev = rot(H - 1, pa, pb);  // p-1 of k = 0 is the previous group's last direction
-        float rcur = rot(0, ra, rb);
+        coef(G == 2 ? -ra : rb, G == 2 ? 0.f : -ra, alp, bep);
+        coef(G == 2 ? -ra : -rb, G == 2 ? 0.f : ra, aln, ben);
+        auto rot = [&](int k, float al, float be) { return al * prm.sth[k] + (be * prm.cth[k] + c0); };
+        // rr(p) = rl(p-1): the edge rate between p-1 and p, carried over k
+        float rr = 0.5f * (rot(0, alc, bec) + rot(H - 1, alp, bep));
+        float rcur = rot(0, alc, bec);
 #pragma unroll
         for (int k = 0; k < H; ++k) {
-          const float rnext = (k + 1 < H) ? rot(k + 1, ra, rb) : rot(0, na, nb);
+          const float rnext = (k + 1 < H) ? rot(k + 1, alc, bec) : rot(0, aln, ben);
           const float rl = 0.5f * (rcur + rnext);  // pl(p) = p+1
-          const float rr = 0.5f * (rcur + rprev);  // pr(p) = p-1
           const float el = (k + 1 < H) ? es[k + 1] : esp;
           const float er = (k > 0) ? es[k - 1] : esm;
-          const float fl = (fmaxf(rl, 0.f) * es[k] + fminf(rl, 0.f) * el - fmaxf(rr, 0.f) * er -
-                            fminf(rr, 0.f) * es[k]) * prm.oneovdth;
-          ef[k] = ice ? 0.f : ef[k] - dtr * fl;
-          rprev = rcur;
+          const float fl = fmaxf(rl, 0.f) * es[k] + fminf(rl, 0.f) * el - fmaxf(rr, 0.f) * er - fminf(rr, 0.f) * es[k];
+          ef[k] = ef[k] - dtrq * fl;
+          rr = rl;
           rcur = rnext;
         }
+      }
+      // sea ice above fice_uth: propagation and refraction leave ef = 0
+      // (umwm_advection.F90:89-97, :170-178)
+      if (ice) {
+#pragma unroll
+        for (int k = 0; k < H; ++k) ef[k] = 0.f;
       }
     }
     // ---- e = ef, and the form-stress integrand with the new spectrum

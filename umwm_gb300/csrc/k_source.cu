@@ -86,16 +86,7 @@ __device__ __forceinline__ Level<H> load_level(const Params& prm, const float* T
 // Sin at direction k of this half; cw = cos(wdir - th(p)) from shared memory.
 __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float U, float cw, float ucs, float vss,
                                        float cp0, float fkovg, bool tail) {
-  float s = U * cw - cp0 - ucs - vss;
-  s = (prm.sin_fac * fabsf(s)) * s;
-  if (s > 0.f) s = s * w.shelt_sf;
-  if (s < 0.f) {
-    s = s * prm.fieldscale1;
-    if (s < 0.f && cw > 0.f) s = s * prm.fieldscale2;
-  }
-  s = (w.c1 * s) * fkovg;
-  if (tail) s = fmaxf(s, 0.f);
-  return s;
+  return sin_fold(prm, w.shelt, U * cw - cp0 - ucs - vss, cw, w.c1 * fkovg, tail);
 }
 
 #ifndef UMWM_INTEG_MINB
@@ -114,9 +105,22 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
 #define UMWM_PHYS_MINB 5  // 96 registers, no spills; measured faster than 4 (128)
 #endif
 
+// Shared memory of one CTA: cos(wdir - th) per lane and direction, and (with
+// SL) the integration's two lagged levels of e and raw Sds.
 template <int G, int H, bool INTEG>
-__global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM_INTEG_SMEM_LAGS && H <= 18 ? UMWM_INTEG_MINB : 3) : UMWM_PHYS_MINB))
-    k_source(const Params prm, const Ptrs P, int compute_rot) {
+struct SrcSmem {
+  static constexpr bool CWS = !(INTEG && UMWM_INTEG_CW_FMA);
+  static constexpr bool SL = INTEG && UMWM_INTEG_SMEM_LAGS && H <= 18;  // within 48 KB of static shared memory
+  float cws[CWS ? H : 1][128];
+  float lag[SL ? 2 : 1][2][SL ? H : 1][128];
+};
+
+// The body of k_source.  SAVE (integration only): this substep also stores
+// its source terms for stress('ocn'); a separate instantiation, so that the
+// substeps that store nothing carry no predicated stores.
+template <int G, int H, bool INTEG, bool SAVE>
+__device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, int compute_rot,
+                                            SrcSmem<G, H, INTEG>& sm) {
   constexpr int PW = 32 / G;   // points per warp
   constexpr int PPC = 4 * PW;  // points per CTA (4 warps)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -137,12 +141,12 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
   const float ra = G == 2 ? (q ? -1.f : 1.f) : (q == 0 ? 1.f : (q == 2 ? -1.f : 0.f));
   const float rb = G == 2 ? 0.f : (q == 1 ? 1.f : (q == 3 ? -1.f : 0.f));
   const float c2s = (G == 4 && (q & 1)) ? -1.f : 1.f;  // cos/sin(2 th) sign of the group
-  constexpr bool CWS = !(INTEG && UMWM_INTEG_CW_FMA);  // cos(wdir - th) table in shared memory
-  __shared__ float cws[CWS ? H : 1][128];
+  constexpr bool CWS = SrcSmem<G, H, INTEG>::CWS;  // cos(wdir - th) table in shared memory
+  auto& cws = sm.cws;
 
   const float dts = INTEG ? ctl->dts : 0.f;
   // the last substep of the dtg keeps its source terms when stress('ocn') is due
-  const bool save = INTEG && P.src_sin && ctl->done && P.glob->save_src;
+  constexpr bool save = INTEG && SAVE;
   const float ustar = P.ustar[jj];
   if (save && valid && q == 0) P.src_ust[j] = ustar;  // the ustar of this substep's sdt
   const WindIn wi = load_wind(prm, P, jj, ja, ustar);
@@ -189,8 +193,8 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
   float mx = 0.f, rmx = 0.f;
   // the current level and the two previous ones (e and raw Sds per direction);
   // with SL the previous two live in shared memory, slot = level & 1
-  constexpr bool SL = INTEG && UMWM_INTEG_SMEM_LAGS && H <= 18;  // within 48 KB of static shared memory
-  __shared__ float lag[SL ? 2 : 1][2][SL ? H : 1][128];
+  constexpr bool SL = SrcSmem<G, H, INTEG>::SL;
+  auto& lag = sm.lag;
   float ec[H], sc[H], e1[SL ? 1 : H], s1[SL ? 1 : H], e2[SL ? 1 : H], s2[SL ? 1 : H];
 #pragma unroll
   for (int k = 0; k < H; ++k) ec[k] = sc[k] = 0.f;
@@ -368,6 +372,21 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
       if (lane == 0) atomicMax(&ctl->maxrot_enc, enc_ord_d(m));
     }
   }
+}
+
+template <int G, int H, bool INTEG>
+__global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM_INTEG_SMEM_LAGS && H <= 18 ? UMWM_INTEG_MINB : 3) : UMWM_PHYS_MINB))
+    k_source(const Params prm, const Ptrs P, int compute_rot) {
+  __shared__ SrcSmem<G, H, INTEG> sm;
+  if (INTEG && P.src_sin) {
+    // the last substep of a step that computes stress('ocn') keeps its source terms
+    const Ctl* ctl = prm.mem[prm.tile_mem[(blockIdx.x * (4 * 32 / G)) / TILE]].ctl;
+    if (ctl->done && P.glob->save_src) {
+      source_body<G, H, INTEG, true>(prm, P, compute_rot, sm);
+      return;
+    }
+  }
+  source_body<G, H, INTEG, false>(prm, P, compute_rot, sm);
 }
 
 template <bool INTEG>

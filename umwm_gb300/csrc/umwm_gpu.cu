@@ -345,6 +345,9 @@ int setup_params(Model& M) {
   p.fieldscale2 = H.fieldscale2; p.twopisds_fac = H.twopisds_fac; p.sds_power = H.sds_power;
   p.inv_sds_power = H.inv_sds_power; p.mss_fac = H.mss_fac; p.snl_fac = H.snl_fac; p.sdt_fac = H.sdt_fac;
   p.bf1 = H.bf1; p.bf2 = H.bf2;
+  p.sin_neg1 = H.sin_fac * H.fieldscale1;
+  // fieldscale2 applies where x fieldscale1 is still negative
+  p.sin_neg2 = H.fieldscale1 > 0.f ? (H.sin_fac * H.fieldscale1) * H.fieldscale2 : p.sin_neg1;
   p.z = H.z; p.nu_air = H.nu_air; p.kappa = H.kappa; p.fprog = H.fprog; p.dth = H.dth; p.dthg = H.dthg;
   p.oneovdth = H.oneovdth; p.dtg = H.dtg; p.fice_lth = H.fice_lth; p.fice_uth = H.fice_uth;
   p.eulerinv = H.eulerinv; p.rhow0 = H.rhow0;
@@ -359,6 +362,8 @@ int setup_params(Model& M) {
   for (int o = 0; o < H.om; ++o) { p.f[o] = H.f[o]; p.dom[o] = H.dom[o]; }
   for (int q = 0; q < H.pm; ++q) {
     p.th[q] = H.th[q]; p.cth[q] = H.cth[q]; p.sth[q] = H.sth[q];
+    p.cthp[q] = std::max(H.cth[q], 0.f); p.cthm[q] = std::min(H.cth[q], 0.f);
+    p.sthp[q] = std::max(H.sth[q], 0.f); p.sthm[q] = std::min(H.sth[q], 0.f);
     p.c2th[q] = (float)std::cos(2.0 * (double)H.th[q]);
     p.s2th[q] = (float)std::sin(2.0 * (double)H.th[q]);
   }
