@@ -102,7 +102,7 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
                              // (frees 9 KB of shared memory; measured no faster at 4, 5 or 6 CTAs)
 #endif
 #ifndef UMWM_PHYS_MINB
-#define UMWM_PHYS_MINB 5  // 96 registers, no spills; measured faster than 4 (128)
+#define UMWM_PHYS_MINB 6  // 80 registers, no spills; measured faster than 5 (96) and 4 (128)
 #endif
 
 // Shared memory of one CTA: cos(wdir - th) per lane and direction, and (with
@@ -145,6 +145,7 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
   auto& cws = sm.cws;
 
   const float dts = INTEG ? ctl->dts : 0.f;
+  const float dtsl2 = dts * 1.44269504f;  // dts log2(e)
   // the last substep of the dtg keeps its source terms when stress('ocn') is due
   constexpr bool save = INTEG && SAVE;
   const float ustar = P.ustar[jj];
@@ -238,12 +239,15 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
         ss2 += __shfl_xor_sync(0xffffffffu, ss2, m);
       }
       const float sA = prm.twopisds_fac * prm.f[o];
+      // Sds = sA (1 + mss_fac chi)^2 (e k4)^sds_power, umwm_source_functions.F90:99-103,
+      // with the level's factors in the exponent: 2^(p log2 e + p log2 k4 + log2 sA)
+      const float lsk = fmaf(prm.sds_power, lg2a(Lc.k4), lg2a(sA));
       if (INTEG || prog) {
 #pragma unroll
         for (int k = 0; k < H; ++k) {
           const float chi = A + Bq * prm.c2th[k] + Cq * prm.s2th[k];
           const float t = 1.f + prm.mss_fac * chi;
-          sc[k] = (sA * (t * t)) * powp(ec[k] * Lc.k4, prm.sds_power);
+          sc[k] = (t * t) * ex2a(fmaf(prm.sds_power, lg2a(ec[k]), lsk));
         }
       }
       if (!INTEG && prog) {
@@ -290,6 +294,7 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
       const float U = wi.wspd + wi.ustar25 * L2.logl2z;
       const float sdt = sdtc * L2.kk;
       const float sice = sv != 0.f ? 2.f * L2.cg0 * sv : 0.f;
+      const float sinkL = ((L2.sbf + sdt) + L2.sdv) - sice;
       float* ES = P.ES + sidx(prm, 0, q * H, jj) + (size_t)Lv * lstride;
       float* EF = P.EF + sidx(prm, 0, q * H, jj) + (size_t)Lv * lstride;
       const size_t so = sidx(prm, 0, q * H, jj) + (size_t)Lv * lstride;  // saved source terms
@@ -300,8 +305,9 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
                                 L2.fkovg, false);
           const float e2k = LAG_E2(k), s2k = LAG_S2(k);
           const float snl = (L2.bf1r * LAG_S1(k)) * LAG_E1(k) + (L2.bf2r * sc[k]) * ec[k] - (prm.snl_fac * s2k) * e2k;
-          const float S = s - s2k * L2.cothkd - L2.sbf - sdt - L2.sdv + sice;
-          const float ef = e2k * ex2a(dts * S * 1.44269504f) + dts * snl;
+          // the level's sinks summed once: S = Sin - Sds coth - (sbf + sdt + sdv - sice)
+          const float S = fmaf(-s2k, L2.cothkd, s) - sinkL;
+          const float ef = e2k * ex2a(dtsl2 * S) + dts * snl;
           if (valid) {
             ES[k * 32] = 0.5f * (LAG_E2(k) + ef);
             EF[k * 32] = ef;
