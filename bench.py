@@ -553,6 +553,8 @@ def main():
     ap.add_argument("--sur-tol", type=float, default=0.02, help="surrogate total-energy budget per substep")
     ap.add_argument("--sur-tol-level", type=float, default=0.1, help="surrogate per-level energy budget")
     ap.add_argument("--members", type=int, default=64)
+    ap.add_argument("--option", action="append", default=[], metavar="NAME=VALUE",
+                    help="library option set after initialize (plain path), e.g. advect_groups=4")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -584,6 +586,9 @@ def main():
     U.clear_inputs()
     case.stage(U)
     U.umwm_initialize(nml_text=case.nml)
+    for opt in args.option:
+        name, value = opt.split("=")
+        U.set_option(name, float(value))
     N = U.dims()["im"]
 
     def advance_to(target):

@@ -66,7 +66,8 @@ struct Params {
   float sin_neg1, sin_neg2;
   int winds, currents, air_density, water_density, seaice, restart, curvilinear, isglobal;
   int ice_possible;  // fice can exceed fice_lth somewhere
-  int groups4;       // spectral kernels use 4 quarter-turn direction groups (option "direction_groups")
+  int groups4;       // source kernels use 4 quarter-turn direction groups (option "direction_groups")
+  int adv_groups4;   // the propagation kernel does (options "direction_groups", "advect_groups")
   float f[MAX_OM], dom[MAX_OM];
   float th[MAX_PM], cth[MAX_PM], sth[MAX_PM], c2th[MAX_PM], s2th[MAX_PM];
   // max(cos th, 0), min(cos th, 0), max(sin th, 0), min(sin th, 0): the

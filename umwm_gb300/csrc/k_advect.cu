@@ -45,8 +45,12 @@ __device__ __forceinline__ float sin_dir(const Params& prm, const WindIn& w, flo
                             // 96 registers with some spilling measured faster than 128 or 168
 #endif
 
+#ifndef UMWM_ADVECT_MINB4
+#define UMWM_ADVECT_MINB4 4  // the same with four quarter-turn groups
+#endif
+
 template <int G, int H, bool CURV>
-__global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(const Params prm, const Ptrs P) {
+__global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_MINB) k_advect(const Params prm, const Ptrs P) {
   constexpr int PW = 32 / G;   // points per warp
   constexpr int PPC = 4 * PW;  // points per CTA (4 warps)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -95,17 +99,25 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(c
     F0 = feup - fwdn + fnup - fsdn;
   }
   const float bx = (vce - vcw), by = (ucn - ucs);
-  // SW: the half-turned group (G = 2, q = 1) reads its east/west and
-  // north/south neighbours swapped, so that both groups use the base
-  // group's upwind weights max/min(cos th0, 0), max/min(sin th0, 0): with
-  // cos th = -cos th0 the east-west flux
-  //   DE (max(c,0) e0 + min(c,0) ee) - DW (max(c,0) ew + min(c,0) e0)
-  // equals the base-direction expression with (DE, ee) and (DW, ew) swapped
-  // (the same for north-south), and the current terms swap with them
-  constexpr bool SW = G == 2 && !CURV;
-  const bool flip = SW && q == 1;
-  const float cA = flip ? -fwup : fedn, cB = flip ? fedn : -fwup;
-  const float cNA = flip ? -fsup : fndn, cSB = flip ? fndn : -fsup;
+  // SW: each group reads its four neighbours in slots chosen so that every
+  // group uses the base group's upwind weights max/min(cos th0, 0) and
+  // max/min(sin th0, 0).  The flux is, per slot pair (A, B) with weights (wp, wm),
+  //   D_A (wp e0 + wm e_A) - D_B (wp e_B + wm e0),
+  // the cos pair (C) and the sin pair (S) summed.  Turned by a half turn
+  // (cos th = -cos th0) the east-west terms of umwm_advection.F90:40-47 are
+  // this with A = west, B = east; turned by a quarter turn (cos th = -sin th0,
+  // sin th = cos th0) the north-south terms are the cos pair (N, S) and the
+  // east-west terms the sin pair (W, E).  Slots: 0 east, 1 west, 2 north,
+  // 3 south; the current terms follow their neighbours.
+  constexpr bool SW = !CURV;
+  const int turn = G == 2 ? 2 * q : q;  // quarter turns of this group
+  const int sCA = turn == 0 ? 0 : turn == 1 ? 2 : turn == 2 ? 1 : 3;
+  const int sCB = turn == 0 ? 1 : turn == 1 ? 3 : turn == 2 ? 0 : 2;
+  const int sSA = turn == 0 ? 2 : turn == 1 ? 1 : turn == 2 ? 3 : 0;
+  const int sSB = turn == 0 ? 3 : turn == 1 ? 0 : turn == 2 ? 2 : 1;
+  auto slot = [](int n, auto e, auto w, auto nn, auto ss) { return n == 0 ? e : n == 1 ? w : n == 2 ? nn : ss; };
+  const float kCA = slot(sCA, fedn, -fwup, fndn, -fsup), kCB = slot(sCB, fedn, -fwup, fndn, -fsup);
+  const float kSA = slot(sSA, fedn, -fwup, fndn, -fsup), kSB = slot(sSB, fedn, -fwup, fndn, -fsup);
 
 #pragma unroll
   for (int k = 0; k < H; ++k) {
@@ -124,8 +136,8 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(c
   const size_t hoff = (size_t)(q * H) * 32;
   const size_t oS = sidx(prm, 0, 0, jj) + hoff, oE = sidx(prm, 0, 0, ie) + hoff, oW = sidx(prm, 0, 0, iw) + hoff,
                oN = sidx(prm, 0, 0, in) + hoff, oSs = sidx(prm, 0, 0, is) + hoff;
-  // the swapped neighbour slots (SW): A/B east-west, NA/SB north-south
-  const size_t oA = flip ? oW : oE, oB = flip ? oE : oW, oNA = flip ? oSs : oN, oSB = flip ? oN : oSs;
+  const size_t oCA = slot(sCA, oE, oW, oN, oSs), oCB = slot(sCB, oE, oW, oN, oSs);
+  const size_t oSA = slot(sSA, oE, oW, oN, oSs), oSB = slot(sSB, oE, oW, oN, oSs);
   // stress_vector_integral divides by cp0 of the previous unrolled point
   // (assumed-shape dummy with lower bound 1 over cp0(:,0:im)),
   // umwm_stress.F90:401, :495-513; the member's first point uses its ghost
@@ -134,7 +146,10 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(c
                tN = tidx(prm, 0, 0, in), tSs = tidx(prm, 0, 0, is), tP = tidx(prm, 0, 0, jprev);
   const float dtaq = 0.25f * dta * oneovar;
   const float dtrq = dtr * prm.oneovdth;
-  const float dyA = flip ? dyw : dye, dyB = flip ? dye : dyw, dxNA = flip ? dxs : dxn, dxSB = flip ? dxn : dxs;
+  const size_t tCA = slot(sCA, tE, tW, tN, tSs), tCB = slot(sCB, tE, tW, tN, tSs);
+  const size_t tSA = slot(sSA, tE, tW, tN, tSs), tSB = slot(sSB, tE, tW, tN, tSs);
+  const float lCA = slot(sCA, dye, dyw, dxn, dxs), lCB = slot(sCB, dye, dyw, dxn, dxs);
+  const float lSA = slot(sSA, dye, dyw, dxn, dxs), lSB = slot(sSB, dye, dyw, dxn, dxs);
 
   float sx = 0.f, sy = 0.f, dsx = 0.f, dsy = 0.f, txom = 0.f, tyom = 0.f;
   // E* and ef of this block two frequencies ahead go to L2 in the background
@@ -170,19 +185,19 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(c
       // ---- propagation, umwm_advection.F90:30-97
       const float cgi = __ldg(T + tS + T_CG0 * 32);
       if (SW) {
-        const float DA = 2.f * (cgi + __ldg(T + (flip ? tW : tE) + T_CG0 * 32)) * dyA;
-        const float DB = 2.f * (cgi + __ldg(T + (flip ? tE : tW) + T_CG0 * 32)) * dyB;
-        const float DNA = 2.f * (cgi + __ldg(T + (flip ? tSs : tN) + T_CG0 * 32)) * dxNA;
-        const float DSB = 2.f * (cgi + __ldg(T + (flip ? tN : tSs) + T_CG0 * 32)) * dxSB;
+        const float DCA = 2.f * (cgi + __ldg(T + tCA + T_CG0 * 32)) * lCA;
+        const float DCB = 2.f * (cgi + __ldg(T + tCB + T_CG0 * 32)) * lCB;
+        const float DSA = 2.f * (cgi + __ldg(T + tSA + T_CG0 * 32)) * lSA;
+        const float DSB = 2.f * (cgi + __ldg(T + tSB + T_CG0 * 32)) * lSB;
 #pragma unroll
         for (int k = 0; k < H; ++k) {
           const float e0 = es[k];
-          const float ea = __ldg(ESo + oA + k * 32), eb = __ldg(ESo + oB + k * 32);
-          const float ena = __ldg(ESo + oNA + k * 32), esb = __ldg(ESo + oSB + k * 32);
+          const float eca = __ldg(ESo + oCA + k * 32), ecb = __ldg(ESo + oCB + k * 32);
+          const float esa = __ldg(ESo + oSA + k * 32), esb = __ldg(ESo + oSB + k * 32);
           const float cp = prm.cthp[k], cm = prm.cthm[k], sp = prm.sthp[k], sm = prm.sthm[k];
-          float flux = DA * (cp * e0 + cm * ea) - DB * (cp * eb + cm * e0) + DNA * (sp * e0 + sm * ena) -
+          float flux = DCA * (cp * e0 + cm * eca) - DCB * (cp * ecb + cm * e0) + DSA * (sp * e0 + sm * esa) -
                        DSB * (sp * esb + sm * e0);
-          if (!zerocur) flux += F0 * e0 + cA * ea + cB * eb + cNA * ena + cSB * esb;
+          if (!zerocur) flux += F0 * e0 + kCA * eca + kCB * ecb + kSA * esa + kSB * esb;
           ef[k] = ef[k] - dtaq * flux;
         }
       }
@@ -328,7 +343,7 @@ __global__ void __launch_bounds__(128, G == 4 ? 4 : UMWM_ADVECT_MINB) k_advect(c
 cudaError_t launch_advect(const Params& prm, const Ptrs& P, cudaStream_t st) {
   const dim3 block(128);
   const bool curv = prm.curvilinear != 0;
-  if (prm.groups4 && quarter_groups(prm.P)) {
+  if (prm.adv_groups4 && quarter_groups(prm.P)) {
     const dim3 grid(prm.ntiles * (TILE / 32));  // 32 points per CTA
     switch (prm.P / 4) {
 #define CASE(X)                                                          \

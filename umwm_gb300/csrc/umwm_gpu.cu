@@ -1668,11 +1668,12 @@ int umwm_gpu_set_option(const char* name, double value) {
     M->ocn_every = value != 0;
     return M->ocn_every ? ensure_ocn(*M) : UMWM_OK;
   }
-  if (s == "direction_groups") {
-    if (value != 2 && value != 4) return fail(UMWM_ERR_ARG, "direction_groups must be 2 or 4");
+  if (s == "direction_groups" || s == "advect_groups") {
+    if (value != 2 && value != 4) return fail(UMWM_ERR_ARG, s + " must be 2 or 4");
     if (value == 4 && !quarter_groups(M->prm.P))
-      return fail(UMWM_ERR_UNSUPPORTED, "direction_groups 4 needs pm % 4 == 0 and pm/4 in {4, 6, 8, 9, 12}");
-    M->prm.groups4 = value == 4 ? 1 : 0;
+      return fail(UMWM_ERR_UNSUPPORTED, s + " 4 needs pm % 4 == 0 and pm/4 in {4, 6, 8, 9, 12}");
+    if (s == "direction_groups") M->prm.groups4 = value == 4 ? 1 : 0;
+    M->prm.adv_groups4 = value == 4 ? 1 : 0;
     // the captured inner loop holds the old launch configuration
     if (M->graph_exec) { cudaGraphExecDestroy(M->graph_exec); M->graph_exec = nullptr; }
     if (M->graph) { cudaGraphDestroy(M->graph); M->graph = nullptr; }
