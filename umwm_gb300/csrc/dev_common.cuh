@@ -87,6 +87,10 @@ __device__ __forceinline__ float sin_fold(const Params& prm, float shelt, float 
   return s;
 }
 
+#ifndef UMWM_PREFETCH_TAB
+#define UMWM_PREFETCH_TAB 1  // the spectral kernels also prefetch the block's table rows two levels ahead
+#endif
+
 // stress_tail, umwm_stress.F90:300-311
 __device__ __forceinline__ float stress_tail(float w, float kmax) {
   const float kcap = 1e3f, a = 0.000112f, b = -0.01451f, c = -1.0186f;

@@ -15,7 +15,9 @@
 // group are the base group's compile-time max/min(cos th0, 0) and
 // max/min(sin th0, 0).  The east/west neighbours sit about one wet column
 // (~nm points) away and are served from L2, which holds the window of blocks
-// the CTAs in flight work on.
+// the CTAs in flight work on; each lane copies the next level's east/west
+// rows into shared memory (cp.async) once this level's propagation has read
+// its own, so they arrive while the refraction and the stress run.
 // Refraction needs E* at p-1 and p+1: inside a group they are registers, at
 // the group's edges they come from the neighbouring groups' lanes (shuffle).  The rotation
 // rate is recomputed from cp0 and the currents (it depends on no spectral
@@ -45,6 +47,20 @@ __device__ __forceinline__ float sin_dir(const Params& prm, const WindIn& w, flo
                             // 96 registers with some spilling measured faster than 128 or 168
 #endif
 
+#ifndef UMWM_ADVECT_STAGE
+#define UMWM_ADVECT_STAGE 1  // east/west neighbour rows staged in shared memory one level ahead
+                             // (two buffers, or the own row staged too, measured slower)
+#endif
+
+// 4-byte asynchronous copy global -> shared (cp.async), its group commit and wait
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 #ifndef UMWM_ADVECT_MINB4
 #define UMWM_ADVECT_MINB4 4  // the same with four quarter-turn groups
 #endif
@@ -69,6 +85,11 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
   const float rb = G == 2 ? 0.f : (q == 1 ? 1.f : (q == 3 ? -1.f : 0.f));
   __shared__ float cws[H][128];
   __shared__ float ccs[CURV ? H : 1][128], scs[CURV ? H : 1][128];
+  // ST: the east/west neighbours' E* rows of the next level are copied into
+  // shared memory (cp.async, per lane) once this level's propagation has
+  // read them, and land while its refraction and stress run
+  constexpr bool ST = G == 2 && !CURV && H <= 18 && UMWM_ADVECT_STAGE;
+  __shared__ float stg[2][ST ? H : 1][128];
 
   const float dta = ctl->dta, dtr = ctl->dtr;
   const bool zerocur = ctl->zerocurrents != 0;
@@ -156,17 +177,35 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
   const size_t blk = sidx(prm, 0, 0, jj & ~31);
   // E* is read only at propagated levels o < oc (the warp's largest oc bounds them)
   const int ocw = (int)__reduce_max_sync(0xffffffffu, (unsigned)max(oc, 0));
+  // (and the block's table rows, which every level reads)
+  const size_t tblk = tidx(prm, 0, 0, jj & ~31);
   auto pf = [&](int o) {
     if (o < O && lane == 0) {
       if (o < ocw) bulk_prefetch(P.ES + blk + (size_t)o * lstride, (unsigned)(prm.P * 128));
       bulk_prefetch(P.EF + blk + (size_t)o * lstride, (unsigned)(prm.P * 128));
+      if (UMWM_PREFETCH_TAB) bulk_prefetch(P.TAB + tblk + (size_t)o * tstride, (unsigned)(T_COUNT * 128));
     }
   };
   pf(0);
   pf(1);
 
+  // copies of level o's east/west rows (the cos slots A, B)
+  auto stage = [&](int o) {
+    if (ST && o < O && o < oc) {
+      const float* ESo = P.ES + (size_t)o * lstride;
+#pragma unroll
+      for (int k = 0; k < (ST ? H : 0); ++k) {
+        cp_async4(&stg[0][ST ? k : 0][threadIdx.x], ESo + oCA + k * 32);
+        cp_async4(&stg[1][ST ? k : 0][threadIdx.x], ESo + oCB + k * 32);
+      }
+    }
+    if (ST) cp_async_commit();
+  };
+  stage(0);
+
   for (int o = 0; o < O; ++o) {
     pf(o + 2);
+    if (ST) cp_async_wait<0>();  // this level's copies have landed
     const float* T = P.TAB + (size_t)o * tstride;
     const float* ESo = P.ES + (size_t)o * lstride;
     const float* EFo = P.EF + (size_t)o * lstride;
@@ -192,7 +231,8 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
 #pragma unroll
         for (int k = 0; k < H; ++k) {
           const float e0 = es[k];
-          const float eca = __ldg(ESo + oCA + k * 32), ecb = __ldg(ESo + oCB + k * 32);
+          const float eca = ST ? stg[0][ST ? k : 0][threadIdx.x] : __ldg(ESo + oCA + k * 32);
+          const float ecb = ST ? stg[1][ST ? k : 0][threadIdx.x] : __ldg(ESo + oCB + k * 32);
           const float esa = __ldg(ESo + oSA + k * 32), esb = __ldg(ESo + oSB + k * 32);
           const float cp = prm.cthp[k], cm = prm.cthm[k], sp = prm.sthp[k], sm = prm.sthm[k];
           float flux = DCA * (cp * e0 + cm * eca) - DCB * (cp * ecb + cm * e0) + DSA * (sp * e0 + sm * esa) -
@@ -201,6 +241,7 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
           ef[k] = ef[k] - dtaq * flux;
         }
       }
+      if (ST) stage(o + 1);  // the buffer has been read
       const float DE = SW ? 0.f : 2.f * (cgi + __ldg(T + tE + T_CG0 * 32)) * dye;
       const float DW = SW ? 0.f : 2.f * (cgi + __ldg(T + tW + T_CG0 * 32)) * dyw;
       const float DN = SW ? 0.f : 2.f * (cgi + __ldg(T + tN + T_CG0 * 32)) * dxn;

@@ -183,9 +183,12 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
   // the dts pre-pass needs only the prognostic levels o < oc (the mss prefix
   // of a level uses the levels below it): the warp stops at its largest oc
   const int OP = INTEG ? O : min(O, (int)__reduce_max_sync(0xffffffffu, (unsigned)max(wi.oc, 0)));
+  const float* Tblk = P.TAB + tidx(prm, 0, 0, jj & ~31);  // this block's table rows
   auto pf = [&](int o) {
-    if (o < OP && lane == 0 && (G == 2 || (w * PW) % 32 == 0))
+    if (o < OP && lane == 0 && (G == 2 || (w * PW) % 32 == 0)) {
       bulk_prefetch_l2(Eblk + (size_t)o * lstride, (unsigned)(prm.P * 128));
+      if (UMWM_PREFETCH_TAB) bulk_prefetch_l2(Tblk + (size_t)o * tstride, (unsigned)(T_COUNT * 128));
+    }
   };
   pf(0);
   pf(1);
