@@ -91,6 +91,16 @@ __device__ __forceinline__ float sin_fold(const Params& prm, float shelt, float 
 #define UMWM_PREFETCH_TAB 1  // the spectral kernels also prefetch the block's table rows two levels ahead
 #endif
 
+// 4-byte asynchronous copy global -> shared (cp.async), its group commit and
+// wait (the wait ends when this thread's copies have landed)
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 // stress_tail, umwm_stress.F90:300-311
 __device__ __forceinline__ float stress_tail(float w, float kmax) {
   const float kcap = 1e3f, a = 0.000112f, b = -0.01451f, c = -1.0186f;

@@ -52,15 +52,6 @@ __device__ __forceinline__ float sin_dir(const Params& prm, const WindIn& w, flo
                              // (two buffers, or the own row staged too, measured slower)
 #endif
 
-// 4-byte asynchronous copy global -> shared (cp.async), its group commit and wait
-__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
 #ifndef UMWM_ADVECT_MINB4
 #define UMWM_ADVECT_MINB4 4  // the same with four quarter-turn groups
 #endif

@@ -97,10 +97,6 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
 #define UMWM_INTEG_SMEM_LAGS 1  // the integration keeps its two lagged levels in shared memory
                                 // (37 KB per CTA): 3.56 ms instead of 4.28 ms with them in registers
 #endif
-#ifndef UMWM_INTEG_CW_FMA
-#define UMWM_INTEG_CW_FMA 0  // 1: the integration forms cos(wdir - th) as cos wdir cos th + sin wdir sin th
-                             // (frees 9 KB of shared memory; measured no faster at 4, 5 or 6 CTAs)
-#endif
 #ifndef UMWM_PHYS_MINB
 #define UMWM_PHYS_MINB 6  // 80 registers, no spills; measured faster than 5 (96) and 4 (128)
 #endif
@@ -109,9 +105,8 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
 // SL) the integration's two lagged levels of e and raw Sds.
 template <int G, int H, bool INTEG>
 struct SrcSmem {
-  static constexpr bool CWS = !(INTEG && UMWM_INTEG_CW_FMA);
   static constexpr bool SL = INTEG && UMWM_INTEG_SMEM_LAGS && H <= 18;  // within 48 KB of static shared memory
-  float cws[CWS ? H : 1][128];
+  float cws[H][128];
   float lag[SL ? 2 : 1][2][SL ? H : 1][128];
 };
 
@@ -141,8 +136,7 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
   const float ra = G == 2 ? (q ? -1.f : 1.f) : (q == 0 ? 1.f : (q == 2 ? -1.f : 0.f));
   const float rb = G == 2 ? 0.f : (q == 1 ? 1.f : (q == 3 ? -1.f : 0.f));
   const float c2s = (G == 4 && (q & 1)) ? -1.f : 1.f;  // cos/sin(2 th) sign of the group
-  constexpr bool CWS = SrcSmem<G, H, INTEG>::CWS;  // cos(wdir - th) table in shared memory
-  auto& cws = sm.cws;
+  auto& cws = sm.cws;  // cos(wdir - th) per lane and direction
 
   const float dts = INTEG ? ctl->dts : 0.f;
   const float dtsl2 = dts * 1.44269504f;  // dts log2(e)
@@ -159,11 +153,8 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
   const float ucg = G == 2 ? ra * wi.uc : ra * wi.uc + rb * wi.vc;
   const float vcg = G == 2 ? ra * wi.vc : ra * wi.vc - rb * wi.uc;
 #pragma unroll
-  for (int k = 0; k < (CWS ? H : 0); ++k) cws[CWS ? k : 0][threadIdx.x] = cosf(wdir - prm.th[q * H + k]);
-  // cos(wdir - th) = cwa cos th0 + cwb sin th0 in the group's frame
-  const float cw0 = cosf(wdir), sw0 = sinf(wdir);
-  const float cwa = ra * cw0 + rb * sw0, cwb = ra * sw0 - rb * cw0;
-#define CW(k) (CWS ? cws[CWS ? (k) : 0][threadIdx.x] : cwa * prm.cth[k] + cwb * prm.sth[k])
+  for (int k = 0; k < H; ++k) cws[k][threadIdx.x] = cosf(wdir - prm.th[q * H + k]);
+#define CW(k) (cws[k][threadIdx.x])
   // own bins only: no barrier needed (each thread reads its own column)
 
   int nie = N, niw = N, nin = N, nis = N;
