@@ -91,6 +91,13 @@ __device__ __forceinline__ float sin_fold(const Params& prm, float shelt, float 
 #define UMWM_PREFETCH_TAB 1  // the spectral kernels also prefetch the block's table rows two levels ahead
 #endif
 
+// 2^x through the SFU (ex2.approx.ftz)
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // 4-byte asynchronous copy global -> shared (cp.async), its group commit and
 // wait (the wait ends when this thread's copies have landed)
 __device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {

@@ -113,7 +113,11 @@ __global__ void k_sice(const Params prm, const Ptrs P) {
   P.sice_v[j] = sv;
 }
 
-// diag, umwm_physics.F90:89-205 (one thread per wet point, reference loop order)
+// diag, umwm_physics.F90:89-205, one thread per wet point.  The bins are
+// visited frequency by frequency (the level's table rows read once), so the
+// sums run in another order than the reference's direction-outer loops; the
+// peak keeps the reference's choice among equal values, the first in its
+// (o fastest, p slowest) order.
 __global__ void k_diag(const Params prm, const Ptrs P) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= prm.Ntot) return;
@@ -126,26 +130,27 @@ __global__ void k_diag(const Params prm, const Ptrs P) {
   float m0 = 0.f, m2 = 0.f, m2k = 0.f, mx = 0.f, my = 0.f, cxx = 0.f, cxy = 0.f, cyy = 0.f, xc = 0.f, yc = 0.f;
   float best = -1.f;
   int op = 0, pp = 0;
-  for (int p = 0; p < NP; ++p) {
-    float mag = 0.f;
-    const float cth = prm.cth[p], sth = prm.sth[p];
-    for (int o = 0; o < O; ++o) {
-      const float e = E[sidx(prm, o, p, j)];
-      const float kdk = tab(T_KDK, o);
+  for (int o = 0; o < O; ++o) {
+    const float kdk = tab(T_KDK, o), k3dk = tab(T_K3DK, o), f2 = prm.f[o] * prm.f[o];
+    const bool pr = o < oc;
+    const float icp = pr ? 1.f / tab(T_CP0, o) : 0.f, cg = pr ? tab(T_CG0, o) : 0.f;
+    const float* Eo = E + sidx(prm, o, 0, j);
+#pragma unroll 4
+    for (int p = 0; p < NP; ++p) {
+      const float cth = prm.cth[p], sth = prm.sth[p];
+      const float e = Eo[p * 32];
       const float ek = e * kdk;
       m0 += ek;
-      m2 += (prm.f[o] * prm.f[o]) * e * kdk;
-      m2k += e * tab(T_K3DK, o);
-      mag += ek;
-      if (ek > best) { best = ek; op = o; pp = p; }
-      if (o < oc) {
-        const float ekc = ek / tab(T_CP0, o);
-        const float cg = tab(T_CG0, o);
+      m2 += (f2 * e) * kdk;
+      m2k += e * k3dk;
+      xc += ek * cth; yc += ek * sth;
+      if (ek > best || (ek == best && p < pp)) { best = ek; op = o; pp = p; }
+      if (pr) {
+        const float ekc = ek * icp;
         mx += ekc * cth; my += ekc * sth;
         cxx += cg * ekc * (cth * cth); cxy += cg * ekc * cth * sth; cyy += cg * ekc * (sth * sth);
       }
     }
-    xc += mag * cth; yc += mag * sth;
   }
   const float rw = P.rhow[ja] * prm.dthg;
   P.mwp[j] = sqrtf(m0 / (m2 + FLT_MIN));
@@ -166,58 +171,85 @@ __global__ void k_diag(const Params prm, const Ptrs P) {
 }
 
 // stokes_drift, umwm_stokes.F90:55-128: util recomputed from k, d and cg0
-// instead of stored (it would be om*im*lm floats).
+// instead of stored (it would be om*im*lm floats).  Per point the
+// direction sums X(o), Y(o) are formed once; the depths are then taken in
+// chunks of SLC with the per-frequency factors computed once per chunk, and
+// the depth-dependent exponentials through ex2 (cosh(x) = (2^(x log2 e) +
+// 2^(-x log2 e)) / 2, which has no cancellation; sinh(kd), which has, stays
+// sinhf).
 __global__ void k_stokes(const Params prm, const Ptrs P) {
+  constexpr int SLC = 8;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= prm.Ntot) return;
   const Member& Mb = prm.mem[prm.tile_mem[j / TILE]];
   if (j >= Mb.ghost) return;
-  const int O = prm.O, NP = prm.P, ldN = prm.ldN;
+  const int O = prm.O, NP = prm.P, ldN = prm.ldN, lm = prm.lm;
   float X[MAX_OM], Y[MAX_OM];
   for (int o = 0; o < O; ++o) {
     float x = 0.f, y = 0.f;
+    const float* Eo = P.E + sidx(prm, o, 0, j);
+#pragma unroll 4
     for (int p = 0; p < NP; ++p) {
-      const float e = P.E[sidx(prm, o, p, j)];
+      const float e = Eo[p * 32];
       x += e * prm.cth[p];
       y += e * prm.sth[p];
     }
     X[o] = x; Y[o] = y;
   }
   const float d = P.d[j];
-  const float twopi = 2.f * 3.14159274f;
+  const float twopi = 2.f * 3.14159274f, log2e = 1.44269504f;
   float um1 = 0.f, usm_prev = 0.f, ds = 0.f, ust_ef = 0.f;
   bool found = false;
-  for (int l = 0; l < prm.lm; ++l) {
-    const float dep = prm.depth[l];
-    float su = 0.f, sv = 0.f;
-    if (!(fabsf(dep) > d)) {
-      for (int o = 0; o < O; ++o) {
-        const float kk = P.TAB[tidx(prm, o, T_K, j)];
-        const float dwn = prm.dom[o] / fabsf(P.TAB[tidx(prm, o, T_CG0, j)]);
-        const float kd = kk * d;
-        const float arg = 2.f * kk * (dep + d);
-        float u;
-        if (fabsf(arg) > 50.f || kd > 50.f)
-          u = twopi * prm.f[o] * 2.f * (kk * kk) * expf(2.f * kk * dep) * dwn * prm.dth;
-        else {
-          const float sh = sinhf(kd);
-          u = twopi * prm.f[o] * (kk * kk) * coshf(2.f * kk * (dep + d)) / (sh * sh) * dwn * prm.dth;
+  for (int l0 = 0; l0 < lm; l0 += SLC) {
+    float su[SLC], sv[SLC];
+#pragma unroll
+    for (int i = 0; i < SLC; ++i) su[i] = sv[i] = 0.f;
+    for (int o = 0; o < O; ++o) {
+      const float kk = P.TAB[tidx(prm, o, T_K, j)];
+      const float dwn = prm.dom[o] / fabsf(P.TAB[tidx(prm, o, T_CG0, j)]);
+      const float kd = kk * d;
+      const float a = ((twopi * prm.f[o]) * (kk * kk)) * dwn * prm.dth;  // util without its depth factor
+      const float sh = sinhf(kd);
+      const float ish2 = kd > 50.f ? 0.f : 1.f / (sh * sh);
+      const float k2l = 2.f * kk * log2e;
+#pragma unroll
+      for (int i = 0; i < SLC; ++i) {
+        const int l = l0 + i;
+        if (l < lm) {
+          const float dep = prm.depth[l];
+          if (!(fabsf(dep) > d)) {
+            const float arg = 2.f * kk * (dep + d);
+            float u;
+            if (fabsf(arg) > 50.f || kd > 50.f) {
+              u = (2.f * a) * ex2_approx(k2l * dep);
+            } else {
+              const float t = k2l * (dep + d);
+              u = a * (0.5f * (ex2_approx(t) + ex2_approx(-t))) * ish2;
+            }
+            su[i] += u * X[o];
+            sv[i] += u * Y[o];
+          }
         }
-        su += u * X[o];
-        sv += u * Y[o];
       }
     }
-    P.us[(size_t)l * ldN + j] = su;
-    P.vs[(size_t)l * ldN + j] = sv;
-    const float um = sqrtf(su * su + sv * sv);
-    if (l == 0) {
-      um1 = um;
-      ust_ef = um1 * prm.eulerinv;
-    } else if (um1 != 0.f && !found && um < ust_ef) {
-      ds = (fabsf(usm_prev - ust_ef) * dep + fabsf(um - ust_ef) * prm.depth[l - 1]) / (usm_prev - um);
-      found = true;
+#pragma unroll
+    for (int i = 0; i < SLC; ++i) {
+      const int l = l0 + i;
+      if (l < lm) {
+        const float dep = prm.depth[l];
+        P.us[(size_t)l * ldN + j] = su[i];
+        P.vs[(size_t)l * ldN + j] = sv[i];
+        const float um = sqrtf(su[i] * su[i] + sv[i] * sv[i]);
+        if (l == 0) {
+          um1 = um;
+          ust_ef = um1 * prm.eulerinv;
+        } else if (um1 != 0.f && !found && um < ust_ef) {
+          ds = (fabsf(usm_prev - ust_ef) * dep + fabsf(um - ust_ef) * prm.depth[l - 1]) / (usm_prev - um);
+          found = true;
+        }
+        usm_prev = um;
+      }
     }
-    usm_prev = um;
   }
   P.ds[j] = -ds;
 }
