@@ -313,8 +313,10 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
           }
         }
       } else {
-        const float oneoverk4 = 1.f / L2.k4;
+        // ef = (num / (sAc t^2 cothkd))^(1/p) / k^4, umwm_physics.F90:73-82, as
+        // 2^((log2 num - 2 log2 t) / p + lt0) with the level's part lt0
         const float sAc = prm.twopisds_fac * prm.f[Lv];
+        const float lt0 = -fmaf(prm.inv_sds_power, lg2a(sAc * L2.cothkd), lg2a(L2.k4));
 #pragma unroll
         for (int k = 0; k < H; ++k) {
           const float s = sin_k(prm, wi, U, CW(k), ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0,
@@ -324,8 +326,7 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
           if (num >= 0.f) {
             const float chi = C2.a + C2.b * prm.c2th[k] + C2.c * prm.s2th[k];
             const float t = 1.f + prm.mss_fac * chi;
-            const float den = (sAc * (t * t)) * L2.cothkd;
-            ef = oneoverk4 * powp(num / den, prm.inv_sds_power);
+            ef = ex2a(fmaf(prm.inv_sds_power, fmaf(-2.f, lg2a(t), lg2a(num)), lt0));
           }
           if (valid) {
             ES[k * 32] = 0.5f * (LAG_E2(k) + ef);
