@@ -303,7 +303,7 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
           const float S = fmaf(-s2k, L2.cothkd, s) - sinkL;
           const float ef = e2k * ex2a(dtsl2 * S) + dts * snl;
           if (valid) {
-            ES[k * 32] = 0.5f * (LAG_E2(k) + ef);
+            ES[k * 32] = 0.5f * (e2k + ef);
             EF[k * 32] = ef;
             if (save) {
               P.src_sin[so + k * 32] = s;
