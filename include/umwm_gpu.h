@@ -202,7 +202,11 @@ int umwm_gpu_get_screen(double* out, long n, long* rows);
  * "direction_groups" (2, default: each point's directions in two half-turn
  * groups per warp lane pair; 4: four quarter-turn groups, fewer registers
  * per thread; needs pm % 4 == 0 and pm/4 in {4, 6, 8, 9, 12}; results differ
- * from 2 by summation order only). */
+ * from 2 by summation order only), "advect_groups" (the same for the
+ * propagation kernel alone), "gust_seed" (seed of the wind gust draws when
+ * the namelist's gustiness > 0, umwm_forcing.F90:49-61; default 1: the
+ * draws are a function of seed, substep, grid cell and component, so a run
+ * repeats with its seed). */
 int umwm_gpu_set_option(const char* name, double value);
 
 /* Run statistics: "substeps", "gpu_ms" (device time of the last run),

@@ -864,6 +864,24 @@ struct Model {
     return true;
   }
 
+  // Wind gust draws in place of Fortran random_number (umwm_forcing.F90:49-56):
+  // uniform [0, 1) from the top 24 bits of a twice-applied SplitMix64
+  // finaliser (Steele, Lea and Flood, 2014) keyed by (seed, substep) and
+  // (cell, component); the same draws as the GPU library makes.
+  static uint64_t splitmix64_mix(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  static float gust_uniform(unsigned seed, unsigned step, unsigned cell, unsigned comp) {
+    const uint64_t key = splitmix64_mix(((uint64_t)seed << 32) | step);
+    const uint64_t z = splitmix64_mix(key ^ (((uint64_t)cell << 1) | comp));
+    return (float)(z >> 40) * (1.f / 16777216.f);
+  }
+  unsigned gust_seed = 1;
+
+  // forcinginterpolate, umwm_forcing.F90:40-99
   void forcinginterpolate() {
     T s = sumt / dtg;
     if (winds) {
@@ -871,6 +889,13 @@ struct Model {
         uw[q] = uwb[q] * (T(1) - sumt / dtg) + uwf[q] * sumt / dtg;
         vw[q] = vwb[q] * (T(1) - sumt / dtg) + vwf[q] * sumt / dtg;
       }
+      if (gustiness > 0)  // :49-61, one draw per cell and component each substep
+        for (size_t q = 0; q < uw.size(); ++q) {
+          const T gu = gustiness * (T(2) * T(gust_uniform(gust_seed, (unsigned)substeps, (unsigned)q, 0)) - T(1));
+          const T gv = gustiness * (T(2) * T(gust_uniform(gust_seed, (unsigned)substeps, (unsigned)q, 1)) - T(1));
+          uw[q] = uw[q] * (T(1) + gu);
+          vw[q] = vw[q] * (T(1) + gv);
+        }
       for (size_t q = 0; q < uw.size(); ++q) {
         wspd_2d[q] = std::sqrt(uw[q] * uw[q] + vw[q] * vw[q]);
         wdir_2d[q] = std::atan2(vw[q], uw[q]);
@@ -1725,6 +1750,7 @@ int oracle_set_option(void* hp, const char* name, double value) {
   auto apply = [&](auto& m) {
     if (n == "max_substeps") { m.max_substeps = (long long)value; m.stopped = false; return 0; }
     if (n == "verbose") { m.verbose = value != 0; return 0; }
+    if (n == "gust_seed") { m.gust_seed = (unsigned)value; return 0; }
     return -1;
   };
   return h->prec == 64 ? apply(*h->f64) : apply(*h->f32);

@@ -297,6 +297,36 @@ def test_oracle_uniform_depth_no_refraction(oracle_mod):
     assert o.scalar("dtr_temp") == o.scalar("dts") or o.scalar("substeps") >= 1
 
 
+def test_oracle_gustiness_draws(oracle_mod):
+    """Wind gustiness in the oracle (umwm_forcing.F90:49-61): the seeded
+    gust draws repeat for the same seed, change with it, and perturb the
+    wind within the gustiness bound."""
+    from umwm_gb300 import configs
+
+    # gusts apply to forcing winds (winds = .true.), as in the reference
+    case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0, gustiness=0.1)
+
+    def run(seed, gust=True):
+        c = case if gust else configs.random_field(mm=48, nm=40, hours=1, dx=2000.0)
+        o = oracle_mod.Oracle(c.nml, 32)
+        c.stage(o)
+        o.initialize()
+        o.set_option("gust_seed", seed)
+        o.set_option("max_substeps", 2)
+        o.run(c.start, c.stop)
+        return o.get("wspd"), o.get("e")
+
+    w7, e7 = run(7)
+    w7b, e7b = run(7)
+    w8, e8 = run(8)
+    w0, _ = run(7, gust=False)
+    assert np.array_equal(w7, w7b) and np.array_equal(e7, e7b)
+    assert not np.array_equal(w7, w8) and not np.array_equal(e7, e8)
+    ratio = w7 / w0
+    assert np.abs(ratio - 1).max() <= 0.1 * np.sqrt(2) + 1e-6  # |1 + gu|, |1 + gv| within 1 +- 0.1
+    assert np.abs(ratio - 1).max() > 0.02
+
+
 def test_oracle_restart_roundtrip(oracle_mod):
     """A restart staged at the start time is read into e and ustar."""
     from umwm_gb300 import configs

@@ -253,3 +253,36 @@ def test_stress_ocn_vs_oracle(U, oracle_mod, which):
     for nx, ny in OCN_PAIRS:
         e = vec_err(got[nx], got[ny], o.get(nx), o.get(ny))
         assert e < tol, "(%s, %s) err %.3g of max" % (nx, ny, e)
+
+
+def test_gustiness_vs_oracle(U, oracle_mod):
+    """Wind gustiness (umwm_forcing.F90:49-61) with the seeded gust draws:
+    the GPU run matches the fp32 oracle, which makes the same draws; the
+    same seed repeats the run bit for bit and another seed changes it."""
+    from umwm_gb300 import configs
+
+    case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0, gustiness=0.1)
+
+    def gpu(seed):
+        U.clear_inputs()
+        case.stage(U)
+        U.umwm_initialize(nml_text=case.nml)
+        U.set_option("gust_seed", seed)
+        U.set_option("max_substeps", 8)
+        U.umwm_run(case.start, case.stop)
+        return U.get_state()[0]
+
+    F7 = gpu(7)
+    o = oracle_mod.Oracle(case.nml, 32)
+    case.stage(o)
+    o.initialize()
+    o.set_option("gust_seed", 7)
+    o.set_option("max_substeps", 8)
+    o.run(case.start, case.stop)
+    _compare_state(U, o, 1e-4, FIELD_TOL)
+    U.umwm_finalize()
+    assert np.array_equal(gpu(7), F7)
+    U.umwm_finalize()
+    F8 = gpu(8)
+    U.umwm_finalize()
+    assert not np.array_equal(F8, F7)

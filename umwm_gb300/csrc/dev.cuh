@@ -64,6 +64,8 @@ struct Params {
   // Sin factors of negative x (sin_fold): sin_fac fieldscale1, and with
   // fieldscale2 where cos(wdir - th) > 0 (umwm_source_functions.F90:60-67)
   float sin_neg1, sin_neg2;
+  float gustiness;      // wind gust amplitude (umwm_forcing.F90:49-61)
+  unsigned gust_seed;   // seed of the gust draws (option "gust_seed")
   int winds, currents, air_density, water_density, seaice, restart, curvilinear, isglobal;
   int ice_possible;  // fice can exceed fice_lth somewhere
   int groups4;       // source kernels use 4 quarter-turn direction groups (option "direction_groups")
@@ -158,6 +160,26 @@ enum OcnField {
   OCN_EPSY_OCN, OCN_EPSX_ATM, OCN_EPSY_ATM, OCN_TAILX, OCN_TAILY, OCN_TAUX1, OCN_TAUY1, OCN_TAUX2, OCN_TAUY2,
   OCN_TAUX3, OCN_TAUY3, OCN_COUNT
 };
+
+// Wind gust draws, umwm_forcing.F90:49-56.  The reference fills gustu and
+// gustv with Fortran random_number once per substep; here draw number
+// (substep, cell, component) is a function of those three and a seed, so a
+// run is reproducible and the oracle makes the same draws: the SplitMix64
+// finaliser (Steele, Lea and Flood, 2014) of the seed and substep keys a
+// second finalising of the cell index (column-major over the 2-d grid, as
+// random_number fills an array) and the component (0: u, 1: v); its top
+// 24 bits are the uniform draw in [0, 1).
+__host__ __device__ inline uint64_t splitmix64_mix(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__host__ __device__ inline float gust_uniform(unsigned seed, unsigned substep, unsigned cell, unsigned comp) {
+  const uint64_t key = splitmix64_mix(((uint64_t)seed << 32) | substep);
+  const uint64_t z = splitmix64_mix(key ^ (((uint64_t)cell << 1) | comp));
+  return (float)(z >> 40) * (1.f / 16777216.f);
+}
 
 // element offsets in the blocked layouts
 __host__ __device__ inline size_t sidx(const Params& prm, int o, int p, int j) {

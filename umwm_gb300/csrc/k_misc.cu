@@ -26,6 +26,12 @@ __global__ void k_prep(const Params prm, const Ptrs P, int compute_rot) {
     if (prm.winds) {
       float uw = M.uwb[q] * a + M.uwf[q] * sumt / dtg;
       float vw = M.vwb[q] * a + M.vwf[q] * sumt / dtg;
+      if (prm.gustiness > 0.f) {  // umwm_forcing.F90:49-61
+        const float gu = prm.gustiness * (2.f * gust_uniform(prm.gust_seed, ctl->substep, q, 0) - 1.f);
+        const float gv = prm.gustiness * (2.f * gust_uniform(prm.gust_seed, ctl->substep, q, 1) - 1.f);
+        uw = uw * (1.f + gu);
+        vw = vw * (1.f + gv);
+      }
       P.wspd[ia] = sqrtf(uw * uw + vw * vw);
       P.wdir[ia] = atan2f(vw, uw);
     }

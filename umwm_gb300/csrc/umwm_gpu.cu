@@ -106,6 +106,7 @@ struct Model {
   bool first = true;
   long long substeps = 0, max_substeps = -1;
   bool verbose = false, check_finite = false, use_graph = false;
+  unsigned gust_seed = 1;  // seed of the wind gust draws (option "gust_seed")
   bool ocn_every = false;  // stress('ocn') after every outer step (option "stress_ocn")
   double last_gpu_ms = 0, last_bins = 0;
   long long launches = 0;
@@ -314,8 +315,8 @@ int setup_params(Model& M) {
     return fail(UMWM_ERR_UNSUPPORTED, "pm must be 4*k with k in {2,3,4,6,8,9,12}");
   if (H.lm > MAX_LM) return fail(UMWM_ERR_UNSUPPORTED, "more than 100 Stokes depths");
   for (const MemberHost& mh : M.mem)
-    if (mh.H.gustiness > 0)
-      return fail(UMWM_ERR_UNSUPPORTED, "gustiness > 0 (Fortran random_number) is not supported");
+    if (mh.H.gustiness != M.mem[0].H.gustiness)
+      return fail(UMWM_ERR_UNSUPPORTED, "ensemble members must share gustiness");
   Params& p = M.prm;
   // layout: each member's wet points, its ghost, padding to a tile
   int off = 0, nmoff = 0;
@@ -345,6 +346,8 @@ int setup_params(Model& M) {
   p.fieldscale2 = H.fieldscale2; p.twopisds_fac = H.twopisds_fac; p.sds_power = H.sds_power;
   p.inv_sds_power = H.inv_sds_power; p.mss_fac = H.mss_fac; p.snl_fac = H.snl_fac; p.sdt_fac = H.sdt_fac;
   p.bf1 = H.bf1; p.bf2 = H.bf2;
+  p.gustiness = H.gustiness;
+  p.gust_seed = M.gust_seed;
   p.sin_neg1 = H.sin_fac * H.fieldscale1;
   // fieldscale2 applies where x fieldscale1 is still negative
   p.sin_neg2 = H.fieldscale1 > 0.f ? (H.sin_fac * H.fieldscale1) * H.fieldscale2 : p.sin_neg1;
@@ -1663,6 +1666,16 @@ int umwm_gpu_set_option(const char* name, double value) {
   if (s == "verbose") { M->verbose = value != 0; return UMWM_OK; }
   if (s == "max_substeps") { M->max_substeps = (long long)value; return UMWM_OK; }
   if (s == "check_finite") { M->check_finite = value != 0; return UMWM_OK; }
+  if (s == "gust_seed") {
+    if (value < 0 || value > 4294967295.0 || value != std::floor(value))
+      return fail(UMWM_ERR_ARG, "gust_seed must be an integer in [0, 2^32)");
+    M->gust_seed = (unsigned)value;
+    M->prm.gust_seed = M->gust_seed;
+    // the captured inner loop holds the old parameters
+    if (M->graph_exec) { cudaGraphExecDestroy(M->graph_exec); M->graph_exec = nullptr; }
+    if (M->graph) { cudaGraphDestroy(M->graph); M->graph = nullptr; }
+    return UMWM_OK;
+  }
   if (s == "use_graph") { M->use_graph = value != 0; return UMWM_OK; }
   if (s == "stress_ocn") {
     M->ocn_every = value != 0;
