@@ -159,6 +159,11 @@ int umwm_gpu_write_restart(const char* path);
  * does. */
 int umwm_gpu_write_output(const char* path);
 
+/* output_spectrum_nc (umwm_io.F90:150-314) has no entry point of its own:
+ * with the namelist's outspec set, umwm_gpu_run appends a record per output
+ * time (and one at the start) to output/umwmspc_<id>_<time>.nc for each
+ * point of namelists/spectrum.nml, when the directory output exists. */
+
 /* Copy a named field into out (n floats).  Names are the reference's
  * variable names: wet-point fields (ht, mwp, mwd, mss, mwl, dwd, dwl, dwp,
  * dcp0, dcp, dcg0, dcg, momx, momy, cgmxx, cgmxy, cgmyy, ustar, cd, taux,
@@ -168,7 +173,8 @@ int umwm_gpu_write_output(const char* path);
  * wdir, uc, vc, rhoa, rhow, rhorat, fice, d, dx, dy), Stokes drift 'us',
  * 'vs' (lm*im, level-major), spectral tables (om*im: k, kdk, k3dk, ...;
  * cp0, cg0 as om*(im+1) with the ghost point first), 'f' (om), 'th' (pm),
- * 'depth' (lm) and the scalars dts, dta, dtr, dtamin, sumt, cgmax, dth.
+ * 'depth' (lm), the 2-d grid fields d_2d, dx_2d, dy_2d, curv, lon, lat
+ * (mm*nm, m fastest) and the scalars dts, dta, dtr, dtamin, sumt, cgmax, dth.
  * The outputs of stress('ocn') (umwm_stress.F90:34-214), over wet points,
  * once it has run (option "stress_ocn", or an outer step with gridded
  * output due): taux_ocntop, tauy_ocntop, taux_ocnbot, tauy_ocnbot, taux_snl,

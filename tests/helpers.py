@@ -48,3 +48,12 @@ def spec_stats(a, b, floor_frac=1e-6):
     m = np.abs(b) > floor_frac * np.abs(b).max()
     r = np.abs(a[m] - b[m]) / np.abs(b[m])
     return l2, float(np.percentile(r, 99.9)), float(r.max())
+
+
+def lonlat_grid(mm, nm, lon0=-80.0, lat0=20.0, dlon=0.05, dlat=0.05, skew=0.002):
+    """A skewed longitude/latitude grid (mm, nm) for gridFromFile cases."""
+    m = np.arange(mm)[:, None]
+    n = np.arange(nm)[None, :]
+    lon = lon0 + dlon * m + skew * n
+    lat = lat0 + dlat * n + 0.5 * skew * m
+    return lon.astype(np.float32), lat.astype(np.float32)

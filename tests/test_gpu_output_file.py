@@ -117,3 +117,101 @@ def test_output_grid_needs_directory(lib_built, tmp_path, monkeypatch):
     U.umwm_finalize()
     assert not os.path.exists("output")
     assert np.isfinite(ht).all()
+
+
+def test_output_spectrum_files(lib_built, tmp_path, monkeypatch):
+    """output_spectrum_nc (umwm_io.F90:150-314): for each wet point listed in
+    namelists/spectrum.nml a file output/umwmspc_<id>_<start>.nc gets one
+    record at the start time and one per outspec hour: the spectrum and the
+    last substep's Sin, Sds, Snl and Sdt at that point, equal to what the C
+    ABI returns.  Points given by longitude/latitude take the nearest cell;
+    land cells write nothing."""
+    scipy_io = pytest.importorskip("scipy.io")
+    from umwm_gb300 import configs
+
+    U = lib_built
+    monkeypatch.chdir(tmp_path)
+    os.makedirs("output")
+    os.makedirs("namelists")
+    case = configs.hurricane(mm=40, nm=36, hours=2, dx=4000.0, dtg=600, seed=3, outspec=1, outgrid=0)
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=case.nml)
+    d = U.dims()
+    ii = U.get_field_i("ii")  # (mm, nm), point number or 0
+    cells = [(m, n) for n in range(2, d["nm"]) for m in range(2, d["mm"])
+             if 1 <= ii[m - 1, n - 1] <= d["im"]]
+    wet1, wet2 = cells[len(cells) // 3], cells[2 * len(cells) // 3]
+    land = [(m, n) for n in range(2, d["nm"]) for m in range(2, d["mm"]) if ii[m - 1, n - 1] == 0]
+    lines = ["XY", "%d %d p1" % wet1, "%d %d p2" % wet2] + (["%d %d dry" % land[0]] if land else [])
+    with open("namelists/spectrum.nml", "w") as f:
+        f.write("\n".join(lines) + "\n")
+    U.umwm_run(case.start, case.stop)
+    lon, lat = U.get_field("lon"), U.get_field("lat")  # (mm, nm)
+    F, _ = U.get_state()
+    src = {v: U.get_field(v) for v in ("ssin", "sds", "snl")}
+    k, sdv, sbf = U.get_field("k"), U.get_field("sdv"), U.get_field("sbf")
+    wspd, wdir = U.get_field("wspd"), U.get_field("wdir")
+    U.umwm_finalize()
+
+    key = case.start.replace(" ", "_")
+    assert sorted(os.listdir("output")) == ["umwmspc_p1_%s.nc" % key, "umwmspc_p2_%s.nc" % key]
+    for pid, (m, n) in (("p1", wet1), ("p2", wet2)):
+        i = ii[m - 1, n - 1] - 1
+        with scipy_io.netcdf_file("output/umwmspc_%s_%s.nc" % (pid, key), "r", mmap=False) as f:
+            assert list(f.variables) == ["frequency", "wavenumber", "direction", "longitude", "latitude", "wspd",
+                                         "wdir", "F", "Sin", "Sds", "Sdt", "Sdv", "Sbf", "Snl"]
+            assert f.dimensions["time"] is None and f.variables["F"].shape == (3, d["pm"], d["om"])
+            np.testing.assert_array_equal(f.variables["F"][-1], F[i])
+            np.testing.assert_array_equal(f.variables["Sin"][-1], src["ssin"][i])
+            np.testing.assert_array_equal(f.variables["Sds"][-1], src["sds"][i])
+            np.testing.assert_array_equal(f.variables["Snl"][-1], src["snl"][i])
+            np.testing.assert_array_equal(f.variables["wavenumber"][:], k[i])
+            np.testing.assert_array_equal(f.variables["Sdv"][:], sdv[i])
+            np.testing.assert_array_equal(f.variables["Sbf"][:], sbf[i])
+            np.testing.assert_array_equal(f.variables["wspd"][-1], [wspd[i]])
+            np.testing.assert_array_equal(f.variables["wdir"][-1], [wdir[i]])
+            sdt = f.variables["Sdt"][:]  # sdt_fac sqrt(rhorat) u* k: proportional to k
+            r = sdt / k[i][None, :]
+            assert np.all(r > 0) and np.allclose(r, r[:, :1], rtol=1e-6)
+            # the records differ in time: the start, +1 h, +2 h
+            assert not np.array_equal(f.variables["F"][0], f.variables["F"][2])
+
+    # on this Cartesian grid lon = lat = 0 (umwm_init.F90:524), so a point
+    # given by longitude/latitude falls on the first cell, a boundary cell:
+    # no file, as in the reference
+    os.remove("output/umwmspc_p1_%s.nc" % key)
+    os.remove("output/umwmspc_p2_%s.nc" % key)
+    with open("namelists/spectrum.nml", "w") as f:
+        f.write("LL\n%.6f %.6f q0\n" % (0.0, 0.0))
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=case.nml)
+    U.set_option("max_substeps", 1)
+    U.umwm_run(case.start, case.stop)
+    U.umwm_finalize()
+    assert os.listdir("output") == []
+
+    # on a lon/lat grid the nearest cell
+    from helpers import lonlat_grid
+
+    case = configs.random_field(mm=40, nm=36, hours=1, gridFromFile=True, outspec=1, outgrid=0)
+    lon, lat = lonlat_grid(40, 36)
+    case.gridtopo["lon"] = lon
+    case.gridtopo["lat"] = lat
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=case.nml)
+    ii = U.get_field_i("ii")
+    m, n = next((m, n) for n in range(10, 30) for m in range(10, 30) if 1 <= ii[m - 1, n - 1] <= U.dims()["im"])
+    glon, glat = U.get_field("lon"), U.get_field("lat")
+    with open("namelists/spectrum.nml", "w") as f:
+        f.write("LL\n%.6f %.6f q1\n" % (glon[m - 1, n - 1] + 1e-4, glat[m - 1, n - 1] - 1e-4))
+    U.set_option("max_substeps", 1)
+    U.umwm_run(case.start, case.stop)
+    U.umwm_finalize()
+    key = case.start.replace(" ", "_")
+    with scipy_io.netcdf_file("output/umwmspc_q1_%s.nc" % key, "r", mmap=False) as f:
+        assert f.variables["longitude"][0] == glon[m - 1, n - 1]
+        assert f.variables["latitude"][0] == glat[m - 1, n - 1]
+        assert f.variables["F"].shape[0] == 1

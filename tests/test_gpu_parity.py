@@ -19,7 +19,7 @@ agree to 2 %.
 import numpy as np
 import pytest
 
-from helpers import rel_err, run_gpu, run_oracle, spec_stats, vec_err
+from helpers import lonlat_grid, rel_err, run_gpu, run_oracle, spec_stats, vec_err
 
 pytestmark = pytest.mark.gpu
 
@@ -122,14 +122,6 @@ def test_cold_start_reference_namelist(U, oracle_mod):
         assert e < 1e-3, "%s rel err %.3g" % (name, e)
 
 
-def _lonlat_grid(mm, nm, lon0=-80.0, lat0=20.0, dlon=0.05, dlat=0.05, skew=0.002):
-    m = np.arange(mm)[:, None]
-    n = np.arange(nm)[None, :]
-    lon = lon0 + dlon * m + skew * n
-    lat = lat0 + dlat * n + 0.5 * skew * m
-    return lon.astype(np.float32), lat.astype(np.float32)
-
-
 @pytest.mark.parametrize("variant", ["ice_attenuation", "ice_cover", "hurricane", "curvilinear", "pm24",
                                      "estuaries"])
 def test_variants(U, oracle_mod, variant):
@@ -148,7 +140,7 @@ def test_variants(U, oracle_mod, variant):
         nsub = 12
     elif variant == "curvilinear":
         case = configs.random_field(mm=40, nm=36, hours=1, gridFromFile=True)
-        lon, lat = _lonlat_grid(40, 36)
+        lon, lat = lonlat_grid(40, 36)
         case.gridtopo["lon"] = lon
         case.gridtopo["lat"] = lat
     elif variant == "pm24":

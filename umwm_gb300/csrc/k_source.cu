@@ -380,9 +380,11 @@ __global__ void __launch_bounds__(128, G == 4 ? (INTEG ? 4 : 5) : (INTEG ? (UMWM
     k_source(const Params prm, const Ptrs P, int compute_rot) {
   __shared__ SrcSmem<G, H, INTEG> sm;
   if (INTEG && P.src_sin) {
-    // the last substep of a step that computes stress('ocn') keeps its source terms
+    // the last substep of a step that computes stress('ocn') or writes output
+    // keeps its source terms, and so does the model's first substep (its
+    // spectrum output)
     const Ctl* ctl = prm.mem[prm.tile_mem[(blockIdx.x * (4 * 32 / G)) / TILE]].ctl;
-    if (ctl->done && P.glob->save_src) {
+    if ((ctl->done || ctl->first) && P.glob->save_src) {
       source_body<G, H, INTEG, true>(prm, P, compute_rot, sm);
       return;
     }

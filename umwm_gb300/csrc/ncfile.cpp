@@ -64,8 +64,8 @@ using File = std::unique_ptr<FILE, FileCloser>;
 }  // namespace
 
 bool write(const std::string& path, const std::vector<std::pair<std::string, size_t>>& dims,
-           const std::vector<Var>& vars, std::string& err) {
-  std::vector<size_t> count(vars.size(), 1);  // elements written (one record for record variables)
+           const std::vector<Var>& vars, std::string& err, size_t numrecs) {
+  std::vector<size_t> count(vars.size(), 1);  // elements per record (all elements for fixed-size variables)
   std::vector<bool> rec(vars.size(), false);
   int nrecdims = 0;
   for (auto& d : dims) {
@@ -102,7 +102,7 @@ bool write(const std::string& path, const std::vector<std::pair<std::string, siz
   auto header = [&](const std::vector<uint64_t>& begin) {
     Buf h;
     h.bytes("CDF\x02", 4);
-    h.u32(any_rec ? 1u : 0u);  // records
+    h.u32(any_rec ? (uint32_t)numrecs : 0u);  // records
     h.u32(TAG_DIM);
     h.u32((uint32_t)dims.size());
     for (auto& d : dims) {
@@ -138,8 +138,8 @@ bool write(const std::string& path, const std::vector<std::pair<std::string, siz
     }
     return h;
   };
-  // data: the fixed-size variables in order, then the one record (each
-  // record variable's slab in order)
+  // data: the fixed-size variables in order, then the records, each the
+  // slabs of the record variables in order
   std::vector<size_t> order;
   for (size_t v = 0; v < vars.size(); ++v)
     if (!rec[v]) order.push_back(v);
@@ -171,10 +171,11 @@ bool write(const std::string& path, const std::vector<std::pair<std::string, siz
   const size_t CH = 1 << 20;
   std::vector<float> vals(CH);
   std::vector<unsigned char> raw(CH * 4);
-  for (size_t v : order) {
-    for (size_t first = 0; first < count[v]; first += CH) {
-      const size_t n = std::min(CH, count[v] - first);
-      if (!vars[v].fill(first, n, vals.data())) {
+  // elements [lo, lo + cnt) of variable v
+  auto put = [&](size_t v, size_t lo, size_t cnt) {
+    for (size_t first = 0; first < cnt; first += CH) {
+      const size_t n = std::min(CH, cnt - first);
+      if (!vars[v].fill(lo + first, n, vals.data())) {
         err = "netCDF write: no data for variable " + vars[v].name;
         return false;
       }
@@ -184,7 +185,13 @@ bool write(const std::string& path, const std::vector<std::pair<std::string, siz
         return false;
       }
     }
-  }
+    return true;
+  };
+  for (size_t v : order)
+    if (!rec[v] && !put(v, 0, count[v])) return false;
+  for (size_t r = 0; any_rec && r < numrecs; ++r)
+    for (size_t v : order)
+      if (rec[v] && !put(v, r * count[v], count[v])) return false;
   if (std::fflush(f.get()) != 0) {
     err = "netCDF write: flush failed on " + path;
     return false;

@@ -107,6 +107,21 @@ struct Model {
   long long substeps = 0, max_substeps = -1;
   bool verbose = false, check_finite = false, use_graph = false;
   unsigned gust_seed = 1;  // seed of the wind gust draws (option "gust_seed")
+  // spectrum output (output_spectrum_nc): the points of namelists/spectrum.nml,
+  // read at the first output, the time of that output (the files' names) and
+  // the records written so far per point (each call rewrites the files)
+  struct SpecPoint {
+    std::string id;
+    int m, n, i;  // grid cell and wet index (1-based)
+  };
+  struct SpecRec {
+    float wspd, wdir;
+    std::vector<float> F, Sin, Sds, Snl, Sdt;
+  };
+  bool spec_read = false;
+  std::vector<SpecPoint> spec_pts;
+  std::string spec_time;
+  std::vector<std::vector<SpecRec>> spec_recs;
   bool ocn_every = false;  // stress('ocn') after every outer step (option "stress_ocn")
   double last_gpu_ms = 0, last_bins = 0;
   long long launches = 0;
@@ -834,6 +849,189 @@ int output_grid(Model& M, const std::string& path) {
   return UMWM_OK;
 }
 
+// The points of namelists/spectrum.nml, umwm_io.F90:178-227: a first line
+// "xy" (grid indices m n, inside the open boundary) or "ll" (longitude,
+// latitude: the nearest cell, the first in column-major order), then one
+// point per line with its identifier.  A missing file means no points; land
+// cells and boundary cells are kept and skipped at output (:229).
+int spectrum_points(Model& M) {
+  M.spec_read = true;
+  M.spec_pts.clear();
+  const HostModel& H = M.mem[0].H;
+  std::FILE* f = std::fopen("namelists/spectrum.nml", "r");
+  if (!f) return UMWM_OK;
+  std::string text;
+  char buf[4096];
+  size_t n;
+  while ((n = std::fread(buf, 1, sizeof buf, f)) > 0) text.append(buf, n);
+  std::fclose(f);
+  std::vector<std::string> lines;
+  size_t a = 0;
+  while (a <= text.size()) {
+    size_t b = text.find('\n', a);
+    if (b == std::string::npos) b = text.size();
+    lines.push_back(text.substr(a, b - a));
+    a = b + 1;
+  }
+  auto fields = [](const std::string& l) {  // list-directed: blanks and commas separate
+    std::vector<std::string> out;
+    std::string cur;
+    for (char c : l) {
+      if (c == ' ' || c == '\t' || c == ',' || c == '\r') {
+        if (!cur.empty()) out.push_back(cur);
+        cur.clear();
+      } else {
+        cur += c;
+      }
+    }
+    if (!cur.empty()) out.push_back(cur);
+    return out;
+  };
+  const std::string mode = lines.empty() ? "" : lines[0].substr(0, std::min<size_t>(2, lines[0].size()));
+  const bool xy = mode == "xy" || mode == "XY", ll = mode == "ll" || mode == "LL";
+  if (!xy && !ll)
+    return fail(UMWM_ERR_INPUT, "output_spectrum_nc: first line in namelists/spectrum.nml must contain "
+                                "\"xy\" (or \"XY\") or \"ll\" (or \"LL\")");
+  for (size_t l = 1; l < lines.size(); ++l) {
+    const std::vector<std::string> w = fields(lines[l]);
+    if (w.size() < 3) continue;
+    Model::SpecPoint sp;
+    sp.id = w[2].substr(0, 40);
+    if (xy) {
+      sp.m = std::atoi(w[0].c_str());
+      sp.n = std::atoi(w[1].c_str());
+      if (sp.m < 2 || sp.m > H.mm - 1 || sp.n < 2 || sp.n > H.nm - 1)
+        return fail(UMWM_ERR_INPUT, "output_spectrum_nc: a requested point in spectrum.nml is out of bounds");
+    } else {
+      const float lo = (float)std::atof(w[0].c_str()), la = (float)std::atof(w[1].c_str());
+      float best = std::numeric_limits<float>::infinity();
+      sp.m = sp.n = 1;
+      for (int nn = 1; nn <= H.nm; ++nn)
+        for (int mm = 1; mm <= H.mm; ++mm) {
+          const float dx = lo - H.lon[H.i2(mm, nn)], dy = la - H.lat[H.i2(mm, nn)];
+          const float d2 = dx * dx + dy * dy;
+          if (d2 < best) {
+            best = d2;
+            sp.m = mm;
+            sp.n = nn;
+          }
+        }
+    }
+    sp.i = H.ii[H.i2(sp.m, sp.n)];
+    M.spec_pts.push_back(sp);
+  }
+  M.spec_recs.assign(M.spec_pts.size(), {});
+  return UMWM_OK;
+}
+
+// output_spectrum_nc, umwm_io.F90:150-314: per wet point of spectrum.nml
+// one file output/umwmspc_<id>_<time of the first output>.nc, one record per
+// output (spectrum F, Sin, Sds after cothkd, Snl and Sdt of the last
+// substep, wspd, wdir) with the static frequency, wavenumber, direction,
+// position, Sdv and Sbf.  The records are kept on the host and each call
+// writes the file again.
+int output_spectrum(Model& M, int64_t t) {
+  int rc;
+  if (!M.spec_read && (rc = spectrum_points(M))) return rc;
+  if (M.spec_time.empty()) M.spec_time = time_to_string(t, '_');
+  const Params& p = M.prm;
+  const MemberHost& mh = M.mem[0];
+  const HostModel& H = mh.H;
+  const int O = p.O, NPd = p.P;
+  const size_t nb = (size_t)O * NPd;
+  const size_t tstride = (size_t)p.NB * T_COUNT * 32;
+  CU(cudaStreamSynchronize(M.st));
+  float* tmp = nullptr;
+  CU(cudaMalloc(&tmp, nb * 4));
+  auto spectrum = [&](const float* src, int j, std::vector<float>& out) {
+    out.resize(nb);
+    cudaError_t e = launch_to_ref(p, src, tmp, j, 1, M.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(M.st);
+    if (e == cudaSuccess) e = cudaMemcpy(out.data(), tmp, nb * 4, cudaMemcpyDeviceToHost);
+    return e;
+  };
+  auto row = [&](int t_, int j, std::vector<float>& out) {  // table row over o at point j
+    out.resize(O);
+    return cudaMemcpy2D(out.data(), 4, M.P.TAB + tidx(p, 0, t_, j), tstride * 4, 4, O, cudaMemcpyDeviceToHost);
+  };
+  cudaError_t e = cudaSuccess;
+  for (size_t s = 0; s < M.spec_pts.size() && e == cudaSuccess; ++s) {
+    const Model::SpecPoint& sp = M.spec_pts[s];
+    if (sp.i < 1 || sp.i > mh.N) continue;  // land or boundary cell (ispec outside istart..iend)
+    const int j = mh.off + sp.i - 1, ja = mh.nmoff + sp.i - 1;
+    Model::SpecRec r;
+    std::vector<float> k, sdv, sbf;
+    float ust = 0.f, rhorat = 0.f;
+    if ((e = spectrum(M.E, j, r.F)) || (e = spectrum(M.P.src_sin, j, r.Sin)) ||
+        (e = spectrum(M.P.src_sds, j, r.Sds)) || (e = spectrum(M.P.src_snl, j, r.Snl)) || (e = row(T_K, j, k)) ||
+        (e = row(T_SDV, j, sdv)) || (e = row(T_SBF, j, sbf)) ||
+        (e = cudaMemcpy(&ust, M.P.src_ust + j, 4, cudaMemcpyDeviceToHost)) ||
+        (e = cudaMemcpy(&rhorat, M.P.rhorat + ja, 4, cudaMemcpyDeviceToHost)) ||
+        (e = cudaMemcpy(&r.wspd, M.P.wspd + ja, 4, cudaMemcpyDeviceToHost)) ||
+        (e = cudaMemcpy(&r.wdir, M.P.wdir + ja, 4, cudaMemcpyDeviceToHost)))
+      break;
+    // Sdt, umwm_source_functions.F90:179-181, with the ustar of that substep
+    const float sdtc = (H.sdt_fac * std::sqrt(rhorat)) * ust;
+    r.Sdt.resize(O);
+    for (int o = 0; o < O; ++o) r.Sdt[o] = sdtc * k[o];
+    M.spec_recs[s].push_back(std::move(r));
+    const std::vector<Model::SpecRec>& recs = M.spec_recs[s];
+    const std::string path = "output/umwmspc_" + sp.id + "_" + M.spec_time + ".nc";
+    std::vector<std::pair<std::string, size_t>> dims = {
+        {"scalar", 1}, {"frequency", (size_t)O}, {"direction", (size_t)NPd}, {"time", 0}};
+    std::vector<nc::Var> vars;
+    auto fixed = [&](const char* name, int dim, std::vector<float> v) {
+      nc::Var x;
+      x.name = name;
+      x.dims = {dim};
+      x.fill = [v](size_t first, size_t n, float* out) {
+        if (first + n > v.size()) return false;
+        std::memcpy(out, v.data() + first, n * 4);
+        return true;
+      };
+      vars.push_back(std::move(x));
+    };
+    // a record variable from a per-record vector (size per record: n1)
+    auto recvar = [&](const char* name, std::vector<int> d, size_t n1, std::function<const float*(const Model::SpecRec&)> get) {
+      nc::Var x;
+      x.name = name;
+      x.dims = d;
+      x.fill = [&recs, n1, get](size_t first, size_t n, float* out) {
+        for (size_t q = 0; q < n; ++q) {
+          const size_t g = first + q, r = g / n1;
+          if (r >= recs.size()) return false;
+          out[q] = get(recs[r])[g % n1];
+        }
+        return true;
+      };
+      vars.push_back(std::move(x));
+    };
+    fixed("frequency", 1, std::vector<float>(H.f.begin(), H.f.begin() + O));
+    fixed("wavenumber", 1, k);
+    fixed("direction", 2, std::vector<float>(H.th.begin(), H.th.begin() + NPd));
+    fixed("longitude", 0, {H.lon[H.i2(sp.m, sp.n)]});
+    fixed("latitude", 0, {H.lat[H.i2(sp.m, sp.n)]});
+    recvar("wspd", {3, 0}, 1, [](const Model::SpecRec& x) { return &x.wspd; });
+    recvar("wdir", {3, 0}, 1, [](const Model::SpecRec& x) { return &x.wdir; });
+    recvar("F", {3, 2, 1}, nb, [](const Model::SpecRec& x) { return x.F.data(); });
+    recvar("Sin", {3, 2, 1}, nb, [](const Model::SpecRec& x) { return x.Sin.data(); });
+    recvar("Sds", {3, 2, 1}, nb, [](const Model::SpecRec& x) { return x.Sds.data(); });
+    recvar("Sdt", {3, 1}, (size_t)O, [](const Model::SpecRec& x) { return x.Sdt.data(); });
+    fixed("Sdv", 1, sdv);
+    fixed("Sbf", 1, sbf);
+    recvar("Snl", {3, 2, 1}, nb, [](const Model::SpecRec& x) { return x.Snl.data(); });
+    std::string err;
+    if (!nc::write(path, dims, vars, err, recs.size())) {
+      std::fprintf(stderr, "umwm: output_spectrum_nc: %s not written (%s)\n", path.c_str(), err.c_str());
+    } else if (M.verbose) {
+      std::printf("umwm: output_spectrum_nc: spectrum written to %s\n", path.c_str());
+    }
+  }
+  cudaFree(tmp);
+  CU(e);
+  return UMWM_OK;
+}
+
 // output/umwmout_<time>.nc; a file that cannot be written is reported and
 // the run goes on, as the reference ignores the netCDF status there
 void write_output_file(Model& M, int64_t t) {
@@ -1010,6 +1208,13 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
   // (umwm_top.F90:121-127), without stress('ocn'): its fields are zero
   bool first_out = M.first && M.mem[0].H.outgrid > 0 && M.mem.size() == 1 && dir_exists("output");
   if (first_out && (rc = ensure_ocn(M))) return rc;
+  // and output/umwmspc_*.nc with that substep's source terms (umwm_top.F90:128)
+  bool first_spec = M.first && M.mem[0].H.outspec > 0 && M.mem.size() == 1 && dir_exists("output");
+  if (first_spec) {
+    if ((rc = ensure_ocn(M))) return rc;
+    static const int one = 1;
+    CU(cudaMemcpyAsync(&M.d_glob->save_src, &one, sizeof(int), cudaMemcpyHostToDevice, M.st));
+  }
   CU(cudaEventRecord(M.ev0, M.st));
   int64_t now = t0;
   while (now < t1) {
@@ -1027,7 +1232,10 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     // exists (the reference's nf90_create fails there silently otherwise);
     // ensembles write none
     const bool grid_write = grid_due && M.mem.size() == 1 && dir_exists("output");
-    const bool ocn_due = M.ocn_every || grid_write;
+    // spectrum output at the times outspec asks for (umwm_top.F90:175-181)
+    const bool spec_due = (H0.outspec > 0 && (sod / 3600) % H0.outspec == 0 && sod % 3600 == 0) || H0.outspec == -1;
+    const bool spec_write = spec_due && M.mem.size() == 1 && dir_exists("output");
+    const bool ocn_due = M.ocn_every || grid_write || spec_write;
     if (ocn_due) {
       if ((rc = ensure_ocn(M))) return rc;
       static const int one = 1;
@@ -1057,6 +1265,12 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
         first_out = false;
         write_output_file(M, t0);
       }
+      if (first_spec) {
+        first_spec = false;
+        if ((rc = output_spectrum(M, t0))) return rc;
+        const int keep = ocn_due ? 1 : 0;  // the step's own stress('ocn') or output still needs them
+        CU(cudaMemcpy(&M.d_glob->save_src, &keep, sizeof(int), cudaMemcpyHostToDevice));
+      }
       CU(cudaMemcpyAsync(M.flag_h, M.d_glob, sizeof(Global), cudaMemcpyDeviceToHost, M.st));
       CU(cudaStreamSynchronize(M.st));
       collect_timings(M);
@@ -1075,6 +1289,7 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
       M.launches++;
     }
     if (grid_write) write_output_file(M, now);
+    if (spec_write && (rc = output_spectrum(M, now))) return rc;
     if (M.verbose) print_screen(M);
     // restart output, umwm_top.F90:183-190 (with the reference's test of
     // outspec == -1 for writing every step)
@@ -1510,8 +1725,13 @@ int umwm_gpu_get_field(const char* name, float* out, long n) {
   if (s == "dtamin") return scalar(H.dtamin);
   if (s == "cgmax") return scalar(H.cgmax);
   if (s == "dth") return scalar(H.dth);
-  if (s == "d_2d" || s == "dx_2d" || s == "dy_2d" || s == "curv") {
-    const std::vector<float>& v = s == "d_2d" ? H.d_2d : s == "dx_2d" ? H.dx_2d : s == "dy_2d" ? H.dy_2d : H.curv;
+  if (s == "d_2d" || s == "dx_2d" || s == "dy_2d" || s == "curv" || s == "lon" || s == "lat") {
+    const std::vector<float>& v = s == "d_2d"    ? H.d_2d
+                                  : s == "dx_2d" ? H.dx_2d
+                                  : s == "dy_2d" ? H.dy_2d
+                                  : s == "lon"   ? H.lon
+                                  : s == "lat"   ? H.lat
+                                                 : H.curv;
     if (need((long)v.size())) return UMWM_ERR_ARG;
     std::copy(v.begin(), v.end(), out);
     return UMWM_OK;

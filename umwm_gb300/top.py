@@ -148,7 +148,7 @@ def get_field(name):
         shape = (pm,)
     elif name == "depth":
         shape = (lm,)
-    elif name in ("d_2d", "dx_2d", "dy_2d", "curv"):
+    elif name in ("d_2d", "dx_2d", "dy_2d", "curv", "lon", "lat"):
         out = np.zeros(mm * nm, dtype=np.float32)
         check(lib().umwm_gpu_get_field(name.encode(), out.ctypes.data_as(_fp), out.size))
         return out.reshape(nm, mm).T
