@@ -203,13 +203,18 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
     float* Eo = P.E + (size_t)o * lstride;
     float ef[H];
 #pragma unroll
-    for (int k = 0; k < H; ++k) ef[k] = EFo[oS + k * 32];  // EF aliases E, written below
+    for (int k = 0; k < H; ++k) ef[k] = EFo[oS + k * 32];  // EF aliases E: e below the cut-off, ef above
     const bool prog = o < oc;
     const unsigned pm = __ballot_sync(0xffffffffu, prog);
     if (prog) {
       float es[H];
 #pragma unroll
       for (int k = 0; k < H; ++k) es[k] = __ldg(ESo + oS + k * 32);
+      // the integration left e here and wrote E* = (e + ef)/2: ef = 2 E* - e.
+      // The explicit step keeps ef/e within about [exp(-explim), exp(explim)],
+      // so the difference loses at most a few ulp of ef
+#pragma unroll
+      for (int k = 0; k < H; ++k) ef[k] = 2.f * es[k] - ef[k];
       const float esm = __shfl_sync(pm, es[H - 1], (lane - PW) & 31);  // E* at p-1 for k = 0 (group q-1)
       const float esp = __shfl_sync(pm, es[0], (lane + PW) & 31);      // E* at p+1 for k = H-1 (group q+1)
       // ---- propagation, umwm_advection.F90:30-97

@@ -29,7 +29,9 @@
 //             also the global max of the rotation rate for refraction's dtr
 //             (umwm_advection.F90:125-154).
 // MODE_INTEG: exponential integration (o <= oc), equilibrium tail (o > oc),
-//             E* = (e + ef)/2 -> ES, ef -> EF (umwm_physics.F90:61-84).
+//             E* = (e + ef)/2 -> ES (umwm_physics.F90:61-84); ef -> EF (= E)
+//             above the cut-off only: below it e stays and the propagation
+//             forms ef = 2 E* - e, which saves a spectrum write per substep.
 #include "dev_common.cuh"
 #include "kernels.hpp"
 
@@ -303,8 +305,8 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
           const float S = fmaf(-s2k, L2.cothkd, s) - sinkL;
           const float ef = e2k * ex2a(dtsl2 * S) + dts * snl;
           if (valid) {
+            // only E*: e stays in place and the propagation forms ef = 2 E* - e
             ES[k * 32] = 0.5f * (e2k + ef);
-            EF[k * 32] = ef;
             if (save) {
               P.src_sin[so + k * 32] = s;
               P.src_sds[so + k * 32] = s2k * L2.cothkd;

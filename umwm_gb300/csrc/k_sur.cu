@@ -138,7 +138,9 @@ __global__ void k_targets(const Params prm, const Ptrs P, const int* pts, int n,
       const int o = c / NP, pr = c - o * NP;
       int p = pr + s;
       if (p >= NP) p -= NP;
-      const float ef = P.EF[sidx(prm, o, p, pts[r])];
+      // ef after the integration: at propagated levels 2 E* - e (e left in place)
+      const size_t a = sidx(prm, o, p, pts[r]);
+      const float ef = o < P.oc[pts[r]] ? 2.f * P.ES[a] - P.EF[a] : P.EF[a];
       t = (logf(fmaxf(ef, 0.f) + EPS) - logf(fmaxf(ecopy[(size_t)r * F0 + c], 0.f) + EPS)) * (1.f / TS);
     }
     T[idx] = __float2bfloat16_rn(t);
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, c
       float sp;
       const float ef = step_bin(prm, P, wi, dts, wdir, ev[u], __bfloat162float(h[o * NP + pr]), o, p, j, sp);
       P.ES[k] = 0.5f * (ev[u] + ef);
-      P.EF[k] = ef;
+      if (o >= wi.oc) P.EF[k] = ef;  // as the integration: E* only at propagated levels
     }
   }
 }
