@@ -3,10 +3,14 @@ the oracle with the same inputs and compare fields."""
 import numpy as np
 
 
-def run_gpu(U, case, max_substeps=-1, start=None, stop=None):
+def run_gpu(U, case, max_substeps=-1, start=None, stop=None, groups=None):
+    """Run the GPU library on a case; groups (2 or 4) fixes the direction
+    mapping of the spectral kernels instead of the size-based default."""
     U.clear_inputs()
     case.stage(U)
     U.umwm_initialize(nml_text=case.nml)
+    if groups is not None:
+        U.set_option("direction_groups", groups)
     U.set_option("max_substeps", max_substeps)
     U.umwm_run(start or case.start, stop or case.stop)
 

@@ -60,11 +60,18 @@ def _compare_state(U, o, tol_spec, tol_field, fields=("ustar", "cd"), vectors=VE
     return err
 
 
-def test_one_substep_fetch_limited(U, oracle_mod):
+# both direction mappings of the spectral kernels: two half-turn groups per
+# point (large domains) and four quarter-turn groups (chosen by size for
+# small ones)
+GROUPS = [2, 4]
+
+
+@pytest.mark.parametrize("groups", GROUPS)
+def test_one_substep_fetch_limited(U, oracle_mod, groups):
     from umwm_gb300 import configs
 
     case = configs.fetch_limited(mm=24, nm=14, hours=1)
-    run_gpu(U, case, max_substeps=1)
+    run_gpu(U, case, max_substeps=1, groups=groups)
     o = run_oracle(oracle_mod, case, 32, max_substeps=1)
     o64 = run_oracle(oracle_mod, case, 64, max_substeps=1)
     assert abs(U.get_field("dts") - o.scalar("dts")) <= 1e-5 * o.scalar("dts")
@@ -72,11 +79,12 @@ def test_one_substep_fetch_limited(U, oracle_mod):
     assert np.array_equal(U.get_field_i("oc"), o.get("oc").astype(np.int32))
 
 
-def test_one_substep_random_field(U, oracle_mod):
+@pytest.mark.parametrize("groups", GROUPS)
+def test_one_substep_random_field(U, oracle_mod, groups):
     from umwm_gb300 import configs
 
     case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0)
-    run_gpu(U, case, max_substeps=1)
+    run_gpu(U, case, max_substeps=1, groups=groups)
     o = run_oracle(oracle_mod, case, 32, max_substeps=1)
     o64 = run_oracle(oracle_mod, case, 64, max_substeps=1)
     assert abs(U.get_field("dts") - o.scalar("dts")) <= 1e-5 * o.scalar("dts")
@@ -84,12 +92,13 @@ def test_one_substep_random_field(U, oracle_mod):
     _compare_state(U, o, SPEC_TOL_1, FIELD_TOL, o64=o64)
 
 
+@pytest.mark.parametrize("groups", GROUPS)
 @pytest.mark.parametrize("nsub", [8])
-def test_substeps_random_field(U, oracle_mod, nsub):
+def test_substeps_random_field(U, oracle_mod, nsub, groups):
     from umwm_gb300 import configs
 
     case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0)
-    run_gpu(U, case, max_substeps=nsub)
+    run_gpu(U, case, max_substeps=nsub, groups=groups)
     o = run_oracle(oracle_mod, case, 32, max_substeps=nsub)
     o64 = run_oracle(oracle_mod, case, 64, max_substeps=nsub)
     _compare_state(U, o, 1e-4, 1e-3, vectors=VECTORS, o64=o64)
@@ -122,9 +131,10 @@ def test_cold_start_reference_namelist(U, oracle_mod):
         assert e < 1e-3, "%s rel err %.3g" % (name, e)
 
 
+@pytest.mark.parametrize("groups", GROUPS)
 @pytest.mark.parametrize("variant", ["ice_attenuation", "ice_cover", "hurricane", "curvilinear", "pm24",
                                      "estuaries"])
-def test_variants(U, oracle_mod, variant):
+def test_variants(U, oracle_mod, variant, groups):
     """Paths the plain configs do not reach: sea ice (Sice and the fice >
     fice_uth zeroing), time-interpolated forcing, a lon/lat grid with
     curvature, another direction count, estuary filling of the mask."""
@@ -156,7 +166,7 @@ def test_variants(U, oracle_mod, variant):
         F = case.restart[1]
         case.restart = (case.restart[0], F[:im] if F.shape[0] >= im else np.resize(F, (im,) + F.shape[1:]),
                         case.restart[2][:im] if case.restart[2].shape[0] >= im else np.resize(case.restart[2], im))
-    run_gpu(U, case, max_substeps=nsub)
+    run_gpu(U, case, max_substeps=nsub, groups=groups)
     o = run_oracle(oracle_mod, case, 32, max_substeps=nsub)
     o64 = run_oracle(oracle_mod, case, 64, max_substeps=nsub)
     assert np.array_equal(U.get_field_i("oc"), o.get("oc").astype(np.int32))

@@ -389,6 +389,10 @@ int setup_params(Model& M) {
   return UMWM_OK;
 }
 
+#ifndef UMWM_AUTO_G4_TILES
+#define UMWM_AUTO_G4_TILES 3
+#endif
+
 int init_device(Model& M) {
   int rc = setup_params(M);
   if (rc) return rc;
@@ -396,6 +400,17 @@ int init_device(Model& M) {
   const int ldN = p.ldN;
   const size_t spec = (size_t)p.O * p.P * ldN;
   if (g_device >= 0) CU(cudaSetDevice(g_device));
+  // Small domains: with fewer than UMWM_AUTO_G4_TILES 64-point tiles per SM
+  // the half-turn mapping leaves SMs idle, and four quarter-turn groups (32
+  // points per CTA) double the CTAs: measured 1.4x at 9.6 k wet points,
+  // 1.3x at 17.7 k, even at 31 k (3.2 tiles per SM), 0.95x at 71 k.  The
+  // options direction_groups / advect_groups override this.
+  {
+    int dev = 0, nsm = 0;
+    CU(cudaGetDevice(&dev));
+    CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    if (quarter_groups(p.P) && (long)p.ntiles < (long)UMWM_AUTO_G4_TILES * nsm) p.groups4 = p.adv_groups4 = 1;
+  }
   M.dev.reset(new Dev());
   Dev& D = *M.dev;
   CU(cudaStreamCreateWithFlags(&M.st, cudaStreamNonBlocking));
