@@ -87,6 +87,12 @@ __device__ __forceinline__ float sin_fold(const Params& prm, float shelt, float 
   return s;
 }
 
+#ifndef UMWM_PF_DIST_SRC
+#define UMWM_PF_DIST_SRC 2  // levels ahead the source kernels prefetch into L2
+#endif
+#ifndef UMWM_PF_DIST_ADV
+#define UMWM_PF_DIST_ADV 2  // levels ahead the propagation prefetches into L2
+#endif
 #ifndef UMWM_PREFETCH_TAB
 #define UMWM_PREFETCH_TAB 1  // the spectral kernels also prefetch the block's table rows two levels ahead
 #endif

@@ -177,8 +177,7 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
       if (UMWM_PREFETCH_TAB) bulk_prefetch(P.TAB + tblk + (size_t)o * tstride, (unsigned)(T_COUNT * 128));
     }
   };
-  pf(0);
-  pf(1);
+  for (int o = 0; o < UMWM_PF_DIST_ADV; ++o) pf(o);
 
   // copies of level o's east/west rows (the cos slots A, B)
   auto stage = [&](int o) {
@@ -195,7 +194,7 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
   stage(0);
 
   for (int o = 0; o < O; ++o) {
-    pf(o + 2);
+    pf(o + UMWM_PF_DIST_ADV);
     if (ST) cp_async_wait<0>();  // this level's copies have landed
     const float* T = P.TAB + (size_t)o * tstride;
     const float* ESo = P.ES + (size_t)o * lstride;
