@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
   const float lSA = slot(sSA, dye, dyw, dxn, dxs), lSB = slot(sSB, dye, dyw, dxn, dxs);
 
   float sx = 0.f, sy = 0.f, dsx = 0.f, dsy = 0.f, txom = 0.f, tyom = 0.f;
-  // E* and ef of this block two frequencies ahead go to L2 in the background
+  // E* and e of this block UMWM_PF_DIST_ADV frequencies ahead go to L2 in the background
   const size_t blk = sidx(prm, 0, 0, jj & ~31);
   // E* is read only at propagated levels o < oc (the warp's largest oc bounds them)
   const int ocw = (int)__reduce_max_sync(0xffffffffu, (unsigned)max(oc, 0));

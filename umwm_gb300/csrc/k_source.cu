@@ -183,7 +183,8 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
       if (UMWM_PREFETCH_TAB) bulk_prefetch_l2(Tblk + (size_t)o * tstride, (unsigned)(T_COUNT * 128));
     }
   };
-  for (int o = 0; o < UMWM_PF_DIST_SRC; ++o) pf(o);
+  constexpr int PFD = INTEG ? UMWM_PF_DIST_INTEG : UMWM_PF_DIST_PHYS;
+  for (int o = 0; o < PFD; ++o) pf(o);
 
   float A = 0.f, B = 0.f, C = 0.f;  // dummy coefficients of the current level
   float mx = 0.f, rmx = 0.f;
@@ -206,7 +207,7 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
 
   const int OL = INTEG ? O + 2 : OP;
   for (int o = 0; o < OL; ++o) {
-    pf(o + UMWM_PF_DIST_SRC);
+    pf(o + PFD);
     if (o < O) {
       const float* r = Eb + (size_t)o * lstride;
 #pragma unroll
