@@ -47,6 +47,10 @@ __device__ __forceinline__ float sin_dir(const Params& prm, const WindIn& w, flo
                             // 96 registers with some spilling measured faster than 128 or 168
 #endif
 
+#ifndef UMWM_ADVECT_HALVES
+#define UMWM_ADVECT_HALVES 1  // each level's directions in two halves (half the row registers)
+#endif
+
 #ifndef UMWM_ADVECT_STAGE
 #define UMWM_ADVECT_STAGE 1  // east/west neighbour rows staged in shared memory one level ahead
                              // (two buffers, or the own row staged too, measured slower)
@@ -193,7 +197,120 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
   };
   stage(0);
 
-  for (int o = 0; o < O; ++o) {
+  // HV: the level's directions in two halves of H/2, so that a lane holds
+  // half a row of e and E* at a time (fewer live registers); the rows at the
+  // halves' edges and the neighbouring groups' edge rows are loaded again
+  constexpr bool HV = UMWM_ADVECT_HALVES && SW && ST && G == 2 && (H % 2 == 0);
+  const size_t oPt = sidx(prm, 0, 0, jj);  // the point's row 0 (all groups)
+  const int pprev = ((q + G - 1) % G) * H + H - 1, pnext = ((q + 1) % G) * H;
+  for (int o = 0; o < (HV ? O : 0); ++o) {
+    pf(o + UMWM_PF_DIST_ADV);
+    if (ST) cp_async_wait<0>();  // this level's copies have landed
+    constexpr int HH = HV ? H / 2 : 1;
+    const float* T = P.TAB + (size_t)o * tstride;
+    const float* ESo = P.ES + (size_t)o * lstride;
+    const float* EFo = P.EF + (size_t)o * lstride;
+    float* Eo = P.E + (size_t)o * lstride;
+    const bool prog = o < oc;
+    const bool refr = prog && o < ocr;
+    float DCA = 0.f, DCB = 0.f, DSA = 0.f, DSB = 0.f;
+    float alc = 0.f, bec = 0.f, alp = 0.f, bep = 0.f, aln = 0.f, ben = 0.f, c0 = 0.f;
+    if (prog) {
+      const float cgi = __ldg(T + tS + T_CG0 * 32);
+      DCA = 2.f * (cgi + __ldg(T + tCA + T_CG0 * 32)) * lCA;
+      DCB = 2.f * (cgi + __ldg(T + tCB + T_CG0 * 32)) * lCB;
+      DSA = 2.f * (cgi + __ldg(T + tSA + T_CG0 * 32)) * lSA;
+      DSB = 2.f * (cgi + __ldg(T + tSB + T_CG0 * 32)) * lSB;
+    }
+    if (refr) {
+      const float gx = 0.5f * (__ldg(T + tE + T_CP0 * 32) - __ldg(T + tW + T_CP0 * 32));
+      const float gy = 0.5f * (__ldg(T + tN + T_CP0 * 32) - __ldg(T + tSs + T_CP0 * 32));
+      c0 = (0.5f * bx) * odx - (0.5f * by) * ody;
+      alc = gx * ra * odx; bec = -(gy * ra * ody);  // this group (G = 2: cb = 0)
+      alp = gx * -ra * odx; bep = -(gy * -ra * ody);  // the other group, both neighbours
+      aln = alp; ben = bep;
+    }
+    auto rot = [&](int k, float al, float be) { return al * prm.sth[k] + (be * prm.cth[k] + c0); };
+    float rr = 0.f, rcur = 0.f;
+    if (refr) {
+      rcur = rot(0, alc, bec);
+      rr = 0.5f * (rcur + rot(H - 1, alp, bep));
+    }
+    const float U = wi.wspd + wi.ustar25 * __ldg(T + tS + T_LOGL2Z * 32);
+    const float cp0 = __ldg(T + tS + T_CP0 * 32), fkovg = __ldg(T + tS + T_FKOVG * 32);
+    const float kdk = __ldg(T + tS + T_KDK * 32);
+    const float icp = 1.f / __ldg(T + tP + T_CP0 * 32);
+    float tx = 0.f, ty = 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k0 = h * HH;
+      float ef[HH];
+#pragma unroll
+      for (int i = 0; i < HH; ++i) ef[i] = EFo[oS + (k0 + i) * 32];  // e below the cut-off, ef above
+      if (prog) {
+        float es[HH];
+#pragma unroll
+        for (int i = 0; i < HH; ++i) es[i] = __ldg(ESo + oS + (k0 + i) * 32);
+#pragma unroll
+        for (int i = 0; i < HH; ++i) ef[i] = 2.f * es[i] - ef[i];  // ef = 2 E* - e
+        // ---- propagation, umwm_advection.F90:30-97
+#pragma unroll
+        for (int i = 0; i < HH; ++i) {
+          const int k = k0 + i;
+          const float e0 = es[i];
+          const float eca = stg[0][ST ? k : 0][threadIdx.x];
+          const float ecb = stg[1][ST ? k : 0][threadIdx.x];
+          const float esa = __ldg(ESo + oSA + k * 32), esb = __ldg(ESo + oSB + k * 32);
+          const float cp = prm.cthp[k], cm = prm.cthm[k], sp = prm.sthp[k], sm = prm.sthm[k];
+          float flux = DCA * (cp * e0 + cm * eca) - DCB * (cp * ecb + cm * e0) + DSA * (sp * e0 + sm * esa) -
+                       DSB * (sp * esb + sm * e0);
+          if (!zerocur) flux += F0 * e0 + kCA * eca + kCB * ecb + kSA * esa + kSB * esb;
+          ef[i] = ef[i] - dtaq * flux;
+        }
+        if (h == 1) stage(o + 1);  // the staged rows have been read
+        // ---- refraction, umwm_advection.F90:122-178
+        if (refr) {
+          // E* beyond this half's edges: the other half, or the other group's edge row
+          const float esL = h == 0 ? __ldg(ESo + oPt + pprev * 32) : __ldg(ESo + oS + (HH - 1) * 32);
+          const float esR = h == 0 ? __ldg(ESo + oS + HH * 32) : __ldg(ESo + oPt + pnext * 32);
+#pragma unroll
+          for (int i = 0; i < HH; ++i) {
+            const int k = k0 + i;
+            const float rnext = (k + 1 < H) ? rot(k + 1, alc, bec) : rot(0, aln, ben);
+            const float rl = 0.5f * (rcur + rnext);
+            const float el = (i + 1 < HH) ? es[i + 1] : esR;
+            const float er = (i > 0) ? es[i - 1] : esL;
+            const float fl = fmaxf(rl, 0.f) * es[i] + fminf(rl, 0.f) * el - fmaxf(rr, 0.f) * er - fminf(rr, 0.f) * es[i];
+            ef[i] = ef[i] - dtrq * fl;
+            rr = rl;
+            rcur = rnext;
+          }
+        }
+        if (ice) {
+#pragma unroll
+          for (int i = 0; i < HH; ++i) ef[i] = 0.f;
+        }
+      }
+      // ---- e = ef, and the form-stress integrand with the new spectrum
+#pragma unroll
+      for (int i = 0; i < HH; ++i) {
+        const int k = k0 + i;
+        ef[i] = ef[i] < 0.f ? 0.f : ef[i];  // NaN stays NaN
+        if (valid && prog) Eo[oS + k * 32] = ef[i];
+        const float s = sin_dir(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], cp0, fkovg, !prog);
+        const float es_ = ef[i] * s;
+        tx += es_ * prm.cth[k];
+        ty += es_ * prm.sth[k];
+      }
+    }
+    tx *= ra * icp;
+    ty *= ra * icp;
+    sx += tx * kdk; sy += ty * kdk;
+    if (o >= oc - 1) { dsx += tx * kdk; dsy += ty * kdk; }
+    if (o == O - 1) { txom = tx; tyom = ty; }
+  }
+
+  for (int o = 0; o < (HV ? 0 : O); ++o) {
     pf(o + UMWM_PF_DIST_ADV);
     if (ST) cp_async_wait<0>();  // this level's copies have landed
     const float* T = P.TAB + (size_t)o * tstride;
