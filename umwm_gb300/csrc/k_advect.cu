@@ -43,12 +43,13 @@ __device__ __forceinline__ float sin_dir(const Params& prm, const WindIn& w, flo
 }
 
 #ifndef UMWM_ADVECT_MINB
-#define UMWM_ADVECT_MINB 5  // resident CTAs per SM the register budget is sized for (two groups):
-                            // 96 registers with some spilling measured faster than 128 or 168
+#define UMWM_ADVECT_MINB 4  // resident CTAs per SM the register budget is sized for (two groups):
+                            // with the rows in halves, 128 registers and no spills measured fastest
+                            // (3.06 ms against 3.25 at 5 CTAs, 3.71 at 6, 3.23 at 3)
 #endif
 
 #ifndef UMWM_ADVECT_HALVES
-#define UMWM_ADVECT_HALVES 1  // each level's directions in two halves (half the row registers)
+#define UMWM_ADVECT_HALVES 2  // each level's directions in this many parts (2: halves; 1: whole rows)
 #endif
 
 #ifndef UMWM_ADVECT_STAGE
@@ -200,13 +201,14 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
   // HV: the level's directions in two halves of H/2, so that a lane holds
   // half a row of e and E* at a time (fewer live registers); the rows at the
   // halves' edges and the neighbouring groups' edge rows are loaded again
-  constexpr bool HV = UMWM_ADVECT_HALVES && SW && ST && G == 2 && (H % 2 == 0);
+  constexpr int NPART = UMWM_ADVECT_HALVES;  // parts of a row (2: halves)
+  constexpr bool HV = NPART > 1 && SW && ST && G == 2 && (H % (NPART > 1 ? NPART : 1) == 0);
   const size_t oPt = sidx(prm, 0, 0, jj);  // the point's row 0 (all groups)
   const int pprev = ((q + G - 1) % G) * H + H - 1, pnext = ((q + 1) % G) * H;
   for (int o = 0; o < (HV ? O : 0); ++o) {
     pf(o + UMWM_PF_DIST_ADV);
     if (ST) cp_async_wait<0>();  // this level's copies have landed
-    constexpr int HH = HV ? H / 2 : 1;
+    constexpr int HH = HV ? H / NPART : 1;
     const float* T = P.TAB + (size_t)o * tstride;
     const float* ESo = P.ES + (size_t)o * lstride;
     const float* EFo = P.EF + (size_t)o * lstride;
@@ -242,7 +244,7 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
     const float icp = 1.f / __ldg(T + tP + T_CP0 * 32);
     float tx = 0.f, ty = 0.f;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < (HV ? NPART : 1); ++h) {
       const int k0 = h * HH;
       float ef[HH];
 #pragma unroll
@@ -267,12 +269,13 @@ __global__ void __launch_bounds__(128, G == 4 ? UMWM_ADVECT_MINB4 : UMWM_ADVECT_
           if (!zerocur) flux += F0 * e0 + kCA * eca + kCB * ecb + kSA * esa + kSB * esb;
           ef[i] = ef[i] - dtaq * flux;
         }
-        if (h == 1) stage(o + 1);  // the staged rows have been read
+        if (h == NPART - 1) stage(o + 1);  // the staged rows have been read
         // ---- refraction, umwm_advection.F90:122-178
         if (refr) {
-          // E* beyond this half's edges: the other half, or the other group's edge row
-          const float esL = h == 0 ? __ldg(ESo + oPt + pprev * 32) : __ldg(ESo + oS + (HH - 1) * 32);
-          const float esR = h == 0 ? __ldg(ESo + oS + HH * 32) : __ldg(ESo + oPt + pnext * 32);
+          // E* beyond this part's edges: the neighbouring parts, or the other
+          // group's edge rows
+          const float esL = h == 0 ? __ldg(ESo + oPt + pprev * 32) : __ldg(ESo + oS + (k0 - 1) * 32);
+          const float esR = h == NPART - 1 ? __ldg(ESo + oPt + pnext * 32) : __ldg(ESo + oS + (k0 + HH) * 32);
 #pragma unroll
           for (int i = 0; i < HH; ++i) {
             const int k = k0 + i;
