@@ -555,7 +555,8 @@ int init_device(Model& M) {
     const HostModel& H = mh.H;
     std::vector<float> uwf_h, vwf_h;
     if ((rc = set_forcing_constants(M, mh))) return rc;
-    if ((rc = read_forcing(M, mh, time_key(H.starttimestr.c_str()), &uwf_h, &vwf_h))) return rc;
+    rc = read_forcing(M, mh, time_key(H.starttimestr.c_str()), &uwf_h, &vwf_h);
+    if (rc) return rc;
     std::vector<float> wspd(mh.N + 1, H.wspd0);
     if (H.winds)
       for (int i = 1; i <= mh.N; ++i) {
@@ -1213,7 +1214,7 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
   int rc;
   if (M.first && M.prm.restart)
     for (size_t m = 0; m < M.mem.size(); ++m)
-      if ((rc = restart_read(M, (int)m, time_key(start.c_str())))) return rc;
+      if ((rc = restart_read(M, (int)m, time_key(start.c_str()))) != UMWM_OK) return rc;
   {
     std::vector<int> sub;
     if ((rc = member_substeps(M, sub))) return rc;
