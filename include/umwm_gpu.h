@@ -205,11 +205,11 @@ int umwm_gpu_get_screen(double* out, long n, long* rows);
  * then runs host-driven), "device" (CUDA device of the next initialize),
  * "stress_ocn" (run stress('ocn') after every outer step: the last substep
  * of each step keeps its source terms, three more spectrum-sized arrays),
- * "direction_groups" (2, default: each point's directions in two half-turn
- * groups per warp lane pair; 4: four quarter-turn groups, fewer registers
- * per thread; needs pm % 4 == 0 and pm/4 in {4, 6, 8, 9, 12}; results differ
- * from 2 by summation order only), "advect_groups" (the same for the
- * propagation kernel alone), "gust_seed" (seed of the wind gust draws when
+ * "direction_groups" (2: each point's directions in two half-turn groups
+ * per warp lane pair; 4: four quarter-turn groups, twice the CTAs; needs
+ * pm % 4 == 0 and pm/4 in {4, 6, 8, 9, 12}; initialize picks 4 below 3
+ * 64-point tiles per SM and 2 above; results differ by summation order
+ * only), "advect_groups" (the same for the propagation kernel alone), "gust_seed" (seed of the wind gust draws when
  * the namelist's gustiness > 0, umwm_forcing.F90:49-61; default 1: the
  * draws are a function of seed, substep, grid cell and component, so a run
  * repeats with its seed). */
