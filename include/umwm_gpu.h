@@ -120,18 +120,18 @@ int umwm_gpu_get_state(float* F, float* ust);
 int umwm_gpu_set_state(const float* F, const float* ust);
 
 /* Same output as umwm_gpu_get_state, for callers that cannot allocate device
- * memory: a coupler checkpointing while a CUDA stream capture is active, a
- * job whose GPU memory is fully committed, or a loop that must not pay
+ * memory at that moment: a job whose GPU memory is fully committed to an
+ * ensemble or a pool allocator, or a coupling loop that must not pay
  * cudaFree's device-wide synchronisation.  umwm_gpu_get_state allocates a
  * temporary device buffer as large as the spectrum (om*pm*im floats); this
  * variant allocates nothing and streams the spectrum to F through a fixed
  * 16 MiB scratch array compiled into the library (held on every GPU that
- * loads the library until the process exits), in chunks of whole wet points.
- * A point's spectrum larger than the scratch (om*pm > 4 Mi floats) is rejected
- * with UMWM_ERR_ARG.  The first call on a device looks up the scratch address
- * there; make it before any stream capture.  All calls share the scratch:
- * calls that overlap on the GPU race.  This entry point has no counterpart in
- * the reference. */
+ * loads the library until the process exits), in chunks of whole wet points,
+ * all on the model's stream.  A point's spectrum larger than the scratch
+ * (om*pm > 4 Mi floats) is rejected with UMWM_ERR_ARG.  The first call on a
+ * device looks up the scratch address there; make it before any stream
+ * capture.  All calls share the scratch: calls that overlap on the GPU race.
+ * This entry point has no counterpart in the reference. */
 int umwm_gpu_get_state_noalloc(float* F, float* ust);
 
 /* restart_write, umwm_restart.F90:59-154: write the selected member's
@@ -216,7 +216,8 @@ int umwm_gpu_get_screen(double* out, long n, long* rows);
 int umwm_gpu_set_option(const char* name, double value);
 
 /* Run statistics: "substeps", "gpu_ms" (device time of the last run),
- * "bin_updates" (wet bins x substeps of the last run), "launches". */
+ * "bin_updates" (wet bins x substeps of the last run), "launches",
+ * "device_free_bytes" (cudaMemGetInfo's free memory of the current device). */
 double umwm_gpu_get_stat(const char* name);
 
 /* Message of the last failure ("" if none). */

@@ -17,6 +17,7 @@
 #include <fstream>
 #include <limits>
 #include <memory>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -1392,11 +1393,10 @@ Model* need_model(bool device) {
 //
 // umwm_gpu_get_state transposes the spectrum into a temporary device buffer as
 // large as the spectrum itself (om*pm*im floats, 4.2 GB on a 1000x1000 grid),
-// allocated and freed on every call.  Some callers cannot do that: a coupler
-// that checkpoints the waves while a CUDA stream capture is active on the
-// device (allocation is not allowed during a global-mode capture), a job whose
+// allocated and freed on every call.  Some callers cannot do that: a job whose
 // GPU memory is fully committed to an ensemble or to another model's pool
-// allocator, or a time-critical loop that must not pay cudaFree's implicit
+// allocator (the temporary would not fit, and a failed checkpoint loses the
+// run), or a time-critical coupling loop that must not pay cudaFree's implicit
 // device-wide synchronisation.  This variant streams the transpose through a
 // fixed scratch area compiled into the library instead.
 //
@@ -1404,8 +1404,9 @@ Model* need_model(bool device) {
 // floats (16 MiB).  Every GPU that loads the library holds it until the
 // process exits.  The spectrum goes through it in chunks of whole wet points
 // (NOALLOC_SCRATCH_FLOATS / (om*pm) points per chunk, 3149 for om=37, pm=36),
-// one transpose launch and one device-to-host copy per chunk.  A single
-// point's spectrum larger than the scratch is rejected with UMWM_ERR_ARG.
+// one transpose launch and one device-to-host copy per chunk, all on the
+// model's stream.  A single point's spectrum larger than the scratch is
+// rejected with UMWM_ERR_ARG.
 //
 // Every call shares the one array and leaves the last chunk in it.  Each chunk
 // is written entirely before it is copied out, so nothing has to start at
@@ -1415,16 +1416,20 @@ Model* need_model(bool device) {
 constexpr size_t NOALLOC_SCRATCH_FLOATS = (size_t)4 << 20;
 static __device__ __align__(256) float g_noalloc_scratch[NOALLOC_SCRATCH_FLOATS];
 
-// per-device address of the scratch array, looked up once per device
+// per-device address of the scratch array, looked up once per device; the
+// lock makes concurrent first calls from several host threads safe (the
+// scratch itself is still shared, see above)
 struct NoallocSlot {
   int device;
   float* ptr;
 };
 std::vector<NoallocSlot> g_noalloc_slots;
+std::mutex g_noalloc_mu;
 
 int noalloc_scratch(float** out) {
   int dev = 0;
   CU(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
   for (const auto& s : g_noalloc_slots)
     if (s.device == dev) {
       *out = s.ptr;
@@ -1439,26 +1444,6 @@ int noalloc_scratch(float** out) {
   g_noalloc_slots.push_back({dev, p});
   *out = p;
   return UMWM_OK;
-}
-
-// transpose of wet points [j0, j0+nj) into the reference order F(om,pm,.)
-__global__ void k_to_ref_chunk(const Params prm, const float* __restrict__ E, float* __restrict__ F, int j0, int nj) {
-  __shared__ float tile[32][33];
-  const int R = prm.O * prm.P;
-  const int c0 = blockIdx.x * 32, jb = blockIdx.y * 32;
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  for (int k = ty; k < 32; k += blockDim.y) {
-    const int c = c0 + k;
-    if (c < R && jb + tx < nj) {
-      const int o = c % prm.O, p = c / prm.O;
-      tile[k][tx] = E[sidx(prm, o, p, j0 + jb + tx)];
-    }
-  }
-  __syncthreads();
-  for (int k = ty; k < 32; k += blockDim.y) {
-    const int jrow = jb + k, c = c0 + tx;
-    if (jrow < nj && c < R) F[(size_t)jrow * R + c] = tile[tx][k];
-  }
 }
 
 }  // namespace
@@ -1664,19 +1649,20 @@ int umwm_gpu_get_state_noalloc(float* F, float* ust) {
   float* scratch = nullptr;
   int rc = noalloc_scratch(&scratch);
   if (rc) return rc;
-  CU(cudaStreamSynchronize(M->st));
   if (F) {
     const int chunk = (int)(NOALLOC_SCRATCH_FLOATS / R);
     for (int j0 = 0; j0 < mh.N; j0 += chunk) {
       const int nj = std::min(chunk, mh.N - j0);
-      dim3 grid((unsigned)((R + 31) / 32), (unsigned)((nj + 31) / 32)), block(32, 8);
-      k_to_ref_chunk<<<grid, block, 0, M->st>>>(p, M->E, scratch, mh.off + j0, nj);
-      CU(cudaGetLastError());
+      CU(launch_to_ref(p, M->E, scratch, mh.off + j0, nj, M->st));
       CU(cudaMemcpyAsync(F + (size_t)j0 * R, scratch, (size_t)nj * R * sizeof(float), cudaMemcpyDeviceToHost, M->st));
+      // the next chunk overwrites the scratch: wait for this copy
       CU(cudaStreamSynchronize(M->st));
     }
   }
-  if (ust) CU(cudaMemcpy(ust, M->P.ustar + mh.off, (size_t)mh.N * 4, cudaMemcpyDeviceToHost));
+  if (ust) {
+    CU(cudaMemcpyAsync(ust, M->P.ustar + mh.off, (size_t)mh.N * 4, cudaMemcpyDeviceToHost, M->st));
+    CU(cudaStreamSynchronize(M->st));
+  }
   return UMWM_OK;
 }
 
@@ -1940,6 +1926,11 @@ double umwm_gpu_get_stat(const char* name) {
   if (s == "gpu_ms") return M->last_gpu_ms;
   if (s == "bin_updates") return M->last_bins;
   if (s == "launches") return (double)M->launches;
+  if (s == "device_free_bytes") {  // cudaMemGetInfo of the current device
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return -1.0;
+    return (double)fr;
+  }
   for (int k = 0; k < K_NK; ++k) {
     if (s == std::string("ms:") + KNAMES[k]) return M->kms[k];
     if (s == std::string("count:") + KNAMES[k]) return (double)M->kcnt[k];
