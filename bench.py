@@ -163,27 +163,63 @@ def traffic_per_bin():
         return {}
 
 
-def cpu_baseline(size, steps, threads):
-    """The oracle (fp32 restatement of the reference, OpenMP over wet points)
-    on a size x size crop of the workload's generator."""
-    from oracle import pyoracle
+ORACLE_FLAGS = {True: "-Ofast -ffast-math %s (the reference's production flags, Makefile:5-6)"
+                      % ("-mcpu=neoverse-v2" if os.uname().machine == "aarch64" else "-march=x86-64-v3"),
+                False: "-O2 -ffp-contract=off (strict IEEE)"}
+
+
+def make_case(name, size):
+    """The plain-path workloads by name, size x size."""
     from umwm_gb300 import configs
 
-    case = configs.random_field(mm=size, nm=size, hours=3)
-    nt = pyoracle.set_threads(threads)
-    o = pyoracle.Oracle(case.nml, 32)
+    if name == "hurricane":
+        return configs.hurricane(mm=size, nm=size, hours=12, seed=3)
+    if name == "fetch_limited":
+        return configs.fetch_limited(mm=size, nm=size, hours=6)
+    return configs.random_field(mm=size, nm=size, hours=3)
+
+
+def oracle_substeps(case, warmup, steps, threads, fast=True, serial_steps=0):
+    """Time the oracle (CPU restatement of the reference, OpenMP over wet
+    points) on a case: `warmup` untimed substeps, then `steps` timed substeps
+    on `threads` host threads, then `serial_steps` more on one thread.
+    Returns (bin-updates/s, threads used, wet points, serial bin-updates/s)."""
+    from oracle import pyoracle
+
+    nt = pyoracle.set_threads(threads, fast)
+    o = pyoracle.Oracle(case.nml, 32, fast=fast)
     case.stage(o)
     o.initialize()
-    o.set_option("max_substeps", 1)  # warm-up substep
-    o.run(case.start, case.stop)
     im = int(o.scalar("im"))
-    o.set_option("max_substeps", 1 + steps)
-    t0 = time.perf_counter()
-    o.run(case.start, case.stop)
-    dt = time.perf_counter() - t0
-    n = int(o.scalar("substeps")) - 1
-    return {"value": n * im * BINS / dt, "unit": UNIT, "cores": nt, "kind": "port",
-            "sample": "random_field %dx%d (%d wet points), %d substeps, fp32 oracle" % (size, size, im, n)}
+
+    def advance(n):
+        done = int(o.scalar("substeps"))
+        target = done + n
+        t0 = time.perf_counter()
+        while done < target:
+            o.set_option("max_substeps", target)
+            o.run(case.start, case.stop)
+            done = int(o.scalar("substeps"))
+        return time.perf_counter() - t0
+
+    advance(warmup)
+    value = steps * im * BINS / advance(steps)
+    serial = None
+    if serial_steps > 0:
+        pyoracle.set_threads(1, fast)
+        serial = serial_steps * im * BINS / advance(serial_steps)
+        pyoracle.set_threads(threads, fast)
+    return value, nt, im, serial
+
+
+def cpu_baseline(case, desc, steps, threads):
+    """The oracle on the bench's own workload (a bounded sample: one warm-up
+    and `steps` timed substeps), built with the reference's production flags."""
+    value, nt, im, _ = oracle_substeps(case, 1, steps, threads, fast=True)
+    return {"value": value, "unit": UNIT, "cores": nt, "kind": "port",
+            "sample": "%d substeps of %s (%d wet points) after one warm-up substep: the oracle (CPU restatement of "
+                      "the reference) built %s, OpenMP over wet points on %d host threads"
+                      % (steps, desc, im, ORACLE_FLAGS[True], nt)}
 
 
 def run_reference(args):
@@ -191,41 +227,25 @@ def run_reference(args):
     if rank != 0:
         return 0
     threads = args.cpu_threads or os.cpu_count() or 1
-    from oracle import pyoracle
-    from umwm_gb300 import configs
-
-    if args.case == "hurricane":
-        case = configs.hurricane(mm=args.ref_size, nm=args.ref_size, hours=12, seed=3)
-    elif args.case == "fetch_limited":
-        case = configs.fetch_limited(mm=args.ref_size, nm=args.ref_size, hours=6)
-    else:
-        case = configs.random_field(mm=args.ref_size, nm=args.ref_size, hours=3)
-    nt = pyoracle.set_threads(threads)
-    o = pyoracle.Oracle(case.nml, 32)
-    case.stage(o)
-    o.initialize()
-    im = int(o.scalar("im"))
-    o.set_option("max_substeps", args.warmup)
-    o.run(case.start, case.stop)
-    done = int(o.scalar("substeps"))
-    target = done + args.steps
-    t0 = time.perf_counter()
-    while done < target:
-        o.set_option("max_substeps", target)
-        o.run(case.start, case.stop)
-        done = int(o.scalar("substeps"))
-    dt = time.perf_counter() - t0
-    value = args.steps * im * BINS / dt
+    size = args.ref_size or args.size
+    case = make_case(args.case, size)
+    value, nt, im, serial = oracle_substeps(case, args.warmup, args.steps, threads, fast=True,
+                                            serial_steps=args.serial_steps)
+    desc = "%s %dx%d" % (args.case, size, size)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * im * BINS / value,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": "%s %dx%d (%d wet points)" % (args.case, args.ref_size, args.ref_size, im),
-                       "wet_points": im, "bins_per_point": BINS},
+            "config": {"workload": "%s (wet points %d, %d bins each), plain path" % (desc, im, BINS),
+                       "wet_points": im, "bins_per_point": BINS, "replicas": 1},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port",
-                             "sample": "%d substeps of %s %dx%d, fp32 oracle (CPU restatement of the reference;"
-                                       " the Fortran reference cannot be built: no Fortran compiler or netCDF)"
-                                       % (args.steps, args.case, args.ref_size, args.ref_size)},
+                             "sample": "%d substeps of %s after %d warm-up substeps: the oracle (CPU restatement of "
+                                       "the reference; the Fortran reference cannot be built here: no Fortran "
+                                       "compiler or netCDF) built %s, OpenMP over wet points on %d host threads"
+                                       % (args.steps, desc, args.warmup, ORACLE_FLAGS[True], nt),
+                             "serial_value": serial,
+                             "serial_sample": ("%d substep(s) of the same run on 1 host thread" % args.serial_steps)
+                             if serial else None},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -537,8 +557,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=1000, help="domain is size x size")
-    ap.add_argument("--ref-size", type=int, default=200, help="crop for the CPU legs")
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--ref-size", type=int, default=0,
+                    help="domain of the reference arm (0: the same as --size)")
+    ap.add_argument("--cpu-steps", type=int, default=2, help="timed substeps of the cpu_baseline leg")
+    ap.add_argument("--serial-steps", type=int, default=1,
+                    help="substeps the reference arm also times on one host thread")
     ap.add_argument("--cpu-threads", type=int, default=0, help="host threads of the CPU legs (0: all)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -572,16 +595,20 @@ def main():
     import umwm_gb300 as U
     from umwm_gb300 import configs
 
+    case = make_case(args.case, args.size)
     if args.case == "hurricane":
-        case = configs.hurricane(mm=args.size, nm=args.size, hours=12, seed=3)
         desc = ("hurricane %dx%d dx=2km (linear shelf 20-3000 m, Holland vortex Vmax 50 m/s Rmax 30 km, 5 m/s, "
                 "0.5 m/s current, 600 s forcing snapshots), plain path" % (args.size, args.size))
     elif args.case == "fetch_limited":
-        case = configs.fetch_limited(mm=args.size, nm=args.size, hours=6)
         desc = "fetch_limited %dx%d dx=5km, 1000 m, 10 m/s, plain path" % (args.size, args.size)
     else:
-        case = configs.random_field(mm=args.size, nm=args.size, hours=3)
         desc = "random_field %dx%d dx=2km, plain path" % (args.size, args.size)
+    # the CPU baseline runs the oracle on this same case before the GPU arm
+    # drops the host copy of its restart spectrum
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(case, "%s %dx%d" % (args.case, args.size, args.size), args.cpu_steps,
+                           os.cpu_count() or 1)
     U.set_option("device", local_rank)
     U.clear_inputs()
     case.stage(U)
@@ -680,9 +707,6 @@ def main():
             "algorithmic_bytes_per_bin": ALGO_BYTES[dom],
             "step_frac_16B": 16.0 * (bins_rank / (gpu_ms / 1e3)) / 1e9 / peak}
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(args.ref_size, args.cpu_steps, os.cpu_count() or 1)
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": nsteps,
             "warmup": args.warmup, "ms_per_step": t_max * 1e3 / nsteps, "higher_is_better": True,

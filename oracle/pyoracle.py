@@ -13,21 +13,23 @@ import subprocess
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-_LIB = None
+_LIBS = {}
 
 
 def build(quiet=True):
-    """Compile oracle/_build/liboracle.so with the committed Makefile."""
+    """Compile oracle/_build/liboracle.so (and the timing-only
+    liboracle_fast.so) with the committed Makefile."""
     out = subprocess.run(["make", "-C", _HERE], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     return os.path.join(_HERE, "_build", "liboracle.so")
 
 
-def lib():
-    global _LIB
-    if _LIB is None:
-        path = os.path.join(_HERE, "_build", "liboracle.so")
+def lib(fast=False):
+    """The strict oracle, or (fast=True) the same source built with the
+    reference's production flags, for timing only."""
+    if fast not in _LIBS:
+        path = os.path.join(_HERE, "_build", "liboracle_fast.so" if fast else "liboracle.so")
         src = os.path.join(_HERE, "umwm_oracle.cpp")
         if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
             build()
@@ -48,12 +50,12 @@ def lib():
         L.oracle_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.c_long]
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         L.oracle_set_threads.restype = ctypes.c_int
-        _LIB = L
-    return _LIB
+        _LIBS[fast] = L
+    return _LIBS[fast]
 
 
-def set_threads(n):
-    return lib().oracle_set_threads(int(n))
+def set_threads(n, fast=False):
+    return lib(fast).oracle_set_threads(int(n))
 
 
 def _f32(a):
@@ -67,10 +69,11 @@ def _fortran_2d(field_mn):
 
 
 class Oracle:
-    """One model instance of the oracle; prec is 32 or 64."""
+    """One model instance of the oracle; prec is 32 or 64.  fast=True loads
+    the timing-only build (the reference's production flags)."""
 
-    def __init__(self, nml_text, prec=32):
-        self.L = lib()
+    def __init__(self, nml_text, prec=32, fast=False):
+        self.L = lib(fast)
         self.prec = prec
         self.h = self.L.oracle_new(int(prec), nml_text.encode())
 

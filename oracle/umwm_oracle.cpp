@@ -195,6 +195,7 @@ struct Model {
     dth = 0, dthg = 0, fieldscale1 = 0, fieldscale2 = 0, inv_sds_power = 0, log10overz = 0, mindelx = 0,
     oneovdth = 0, sumt = 0, twopisds_fac = 0, twonu = 0, dtr_temp = 0;
   long long substeps = 0, max_substeps = -1;
+  long long cut_count = 0;  // bins whose negative ef was cut to 0 (see run)
   bool stopped = false;
 
   // 2-d (mm,nm), Fortran order
@@ -1485,10 +1486,12 @@ struct Model {
         // e = ef (umwm_top.F90:113), with negatives cut to 0 as the GPU path
         // does: the explicit Snl term can leave a tiny negative ef, after
         // which (e k^4)^sds_power is NaN (seen in fp64 on the hurricane case)
+        // cut_count: the bins this cut changed since initialize
         for (int q = istart; q <= iend; ++q)
           for (int p = 1; p <= pm; ++p)
             for (int o = 1; o <= om; ++o) {
               const T v = ef[opi(o, p, q)];
+              if (v < T(0)) ++cut_count;
               e[opi(o, p, q)] = v < T(0) ? T(0) : v;
             }
         stress_atm();
@@ -1580,7 +1583,7 @@ bool get_field(M& m, const std::string& name, double* out, long n) {
       {"bf2", (double)m.bf2}, {"im", (double)m.im}, {"imm", (double)m.imm}, {"lm", (double)m.lm},
       {"iip", (double)m.iip}, {"substeps", (double)m.substeps}, {"dtr_temp", (double)m.dtr_temp},
       {"first", (double)m.first}, {"om", (double)m.om}, {"pm", (double)m.pm}, {"mm", (double)m.mm},
-      {"nm", (double)m.nm}, {"zerocurrents", (double)m.zerocurrents}};
+      {"nm", (double)m.nm}, {"zerocurrents", (double)m.zerocurrents}, {"cut_count", (double)m.cut_count}};
   if (sc.count(name)) { if (n < 1) return false; out[0] = sc[name]; return true; }
   if (name == "screen") {
     if (n < (long)m.screen.size()) return false;

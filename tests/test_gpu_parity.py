@@ -288,3 +288,59 @@ def test_gustiness_vs_oracle(U, oracle_mod):
     F8 = gpu(8)
     U.umwm_finalize()
     assert not np.array_equal(F8, F7)
+
+
+@pytest.mark.parametrize("which", ["random_field", "hurricane"])
+def test_stokes_drift_vs_oracle(U, oracle_mod, which):
+    """The Stokes drift profile us, vs at every depth level and its e-folding
+    depth ds (umwm_stokes.F90:92-128) after several outer steps, against the
+    fp32 oracle (to 1e-3 of the level's largest drift, ds to 1e-3 relative)
+    and against the fp64 oracle (no further from it than 2x the fp32
+    oracle's own error plus 1e-4 of the level's largest drift: on the
+    hurricane the GPU and fp32 spectra drift apart by ~3e-5 relative L2 in
+    the hour, and the drift is a weighted sum of them)."""
+    from umwm_gb300 import configs
+
+    if which == "random_field":
+        case = configs.random_field(mm=48, nm=40, hours=3, dx=2000.0)
+    else:
+        case = configs.hurricane(mm=40, nm=36, hours=1, dx=4000.0, dtg=600)
+    run_gpu(U, case)
+    us, vs, ds = U.get_field("us"), U.get_field("vs"), U.get_field("ds")
+    U.umwm_finalize()
+    o = run_oracle(oracle_mod, case, 32)
+    o64 = run_oracle(oracle_mod, case, 64)
+    assert us.shape == o.get("us").shape and np.abs(us).max() > 0
+    for lv in range(us.shape[0]):
+        e = vec_err(us[lv], vs[lv], o.get("us")[lv], o.get("vs")[lv])
+        assert e < 1e-3, "level %d: (us, vs) err %.3g of max" % (lv, e)
+        g = vec_err(us[lv], vs[lv], o64.get("us")[lv], o64.get("vs")[lv])
+        c = vec_err(o.get("us")[lv], o.get("vs")[lv], o64.get("us")[lv], o64.get("vs")[lv])
+        assert g <= 2 * c + 1e-4, "level %d: GPU err vs fp64 %.3g > 2 x fp32 oracle's %.3g" % (lv, g, c)
+    e = rel_err(ds, o.get("ds"), 1e-6)
+    assert e < 1e-3, "ds rel err %.3g" % e
+    e64 = rel_err(ds, o64.get("ds"), 1e-6)
+    c64 = rel_err(o.get("ds"), o64.get("ds"), 1e-6)
+    assert e64 <= 2 * c64 + 1e-4, "ds err vs fp64 %.3g > 2 x fp32 oracle's %.3g" % (e64, c64)
+
+
+@pytest.mark.parametrize("groups", GROUPS)
+def test_global_domain(U, oracle_mod, groups):
+    """A periodic (isGlobal) domain: the west neighbour of the m = 1 column is
+    m = mm and the east neighbour of m = mm is m = 1 (umwm_init.F90:993-1007),
+    so propagation and refraction cross the seam.  Several substeps on the
+    GPU against the fp32 and fp64 oracle, both direction mappings."""
+    from umwm_gb300 import configs
+
+    case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0, isGlobal=True)
+    run_gpu(U, case, max_substeps=8, groups=groups)
+    # the seam is wet somewhere: a point on m = 1 whose west neighbour is on m = mm
+    mi, iw = U.get_field_i("mi"), U.get_field_i("iw")
+    im = U.dims()["im"]
+    seam = [i for i in range(im) if mi[i] == 1 and iw[i] > 0 and mi[iw[i] - 1] == 48]
+    assert len(seam) > 5
+    o = run_oracle(oracle_mod, case, 32, max_substeps=8)
+    o64 = run_oracle(oracle_mod, case, 64, max_substeps=8)
+    assert np.array_equal(U.get_field_i("oc"), o.get("oc").astype(np.int32))
+    _compare_state(U, o, 1e-4, 1e-3, vectors=VECTORS, o64=o64)
+    U.umwm_finalize()

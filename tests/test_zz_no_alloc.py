@@ -40,7 +40,7 @@ def test_get_state_noalloc_matches_get_state(lib_built):
         assert F.shape == F_ref.shape
         np.testing.assert_array_equal(F, F_ref)
         np.testing.assert_array_equal(u, u_ref)
-        free = U.get_stat("device_free_bytes")
+        free = U.stat("device_free_bytes")
         assert free > 0
         if free0 is None:
             free0 = free  # after the first call: the scratch address is resolved

@@ -194,7 +194,9 @@ def random_field(mm=1000, nm=1000, hours=3, dx=2000.0, seed=2, hs=0.2, fp=0.3, l
     vc = (cv / cs.max()).astype(np.float32)
     start = "2012-01-01 00:00:00"
     stop = _time_str(start, hours * 3600)
-    mask = sea_mask_from_z(z)
+    # a global (periodic in m) domain keeps its m = 1 and m = mm rows wet
+    isglobal = bool({k.lower(): v for k, v in nml.items()}.get("isglobal", False))
+    mask = sea_mask_from_z(z, isglobal)
     wm, wn = unroll(mask)
     if len(wm) == 0:
         raise ValueError("random_field: no wet point")
