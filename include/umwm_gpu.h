@@ -212,12 +212,30 @@ int umwm_gpu_get_screen(double* out, long n, long* rows);
  * only), "advect_groups" (the same for the propagation kernel alone), "gust_seed" (seed of the wind gust draws when
  * the namelist's gustiness > 0, umwm_forcing.F90:49-61; default 1: the
  * draws are a function of seed, substep, grid cell and component, so a run
- * repeats with its seed). */
+ * repeats with its seed), "phys_groups" / "integ_groups" (the mapping of the
+ * dts pre-pass or the integration alone), "minb_phys" / "minb_integ" /
+ * "minb_advect" (resident CTAs per SM the kernel's register budget is sized
+ * for; 0 or a budget without a compiled instance: the default) and
+ * "pf_phys" / "pf_integ" / "pf_advect" (frequency levels each kernel
+ * prefetches into L2 ahead), "autotune" (0 off; 1: from the next substep
+ * on, time the register budgets and prefetch distances of the three
+ * spectral kernels on the model's own substeps, round-robin, and keep the
+ * fastest of each; results do not change; 2: also the direction mappings,
+ * which changes results by rounding only; choices are cached per domain
+ * shape for the life of the process), "count_cut" (1: count the bins
+ * whose negative ef the propagation cuts to 0 before e = ef, read with
+ * umwm_gpu_get_stat "cut_count"; pm = 36 only).  This library's own options
+ * have no counterpart in the reference. */
 int umwm_gpu_set_option(const char* name, double value);
 
 /* Run statistics: "substeps", "gpu_ms" (device time of the last run),
  * "bin_updates" (wet bins x substeps of the last run), "launches",
- * "device_free_bytes" (cudaMemGetInfo's free memory of the current device). */
+ * "device_free_bytes" (cudaMemGetInfo's free memory of the current device),
+ * "cut_count" (bins the non-negativity cut changed since option
+ * "count_cut" was set), "autotune_active", "autotune_done",
+ * "autotune_substeps" (substeps measured),
+ * "config:phys" / "config:integ" / "config:advect" (launch configuration in
+ * use: direction groups * 100 + CTAs per SM * 10 + prefetch levels). */
 double umwm_gpu_get_stat(const char* name);
 
 /* Message of the last failure ("" if none). */

@@ -43,6 +43,20 @@ enum TableRow {
 
 constexpr int TILE = 64;  // wet points of a tile (a member's points start on a tile boundary)
 
+// default levels ahead the spectral kernels prefetch the spectrum (and table)
+// rows into L2 (Params::pf_*, tunable); measured on 1000x1000: the
+// integration and the propagation are fastest at one level (two: +3 % and
+// +5 %, four: +13 % and +8 %), the dts pre-pass at two
+#ifndef UMWM_PF_DIST_PHYS
+#define UMWM_PF_DIST_PHYS 2
+#endif
+#ifndef UMWM_PF_DIST_INTEG
+#define UMWM_PF_DIST_INTEG 1
+#endif
+#ifndef UMWM_PF_DIST_ADV
+#define UMWM_PF_DIST_ADV 1
+#endif
+
 // Direction groups per point of the spectral kernels: 4 quarter-turn groups
 // when pm % 4 == 0 and pm/4 is a supported group size, else 2 half-turn groups.
 __host__ __device__ constexpr bool quarter_groups(int pm) {
@@ -68,8 +82,17 @@ struct Params {
   unsigned gust_seed;   // seed of the gust draws (option "gust_seed")
   int winds, currents, air_density, water_density, seaice, restart, curvilinear, isglobal;
   int ice_possible;  // fice can exceed fice_lth somewhere
-  int groups4;       // source kernels use 4 quarter-turn direction groups (option "direction_groups")
+  int groups4;       // the integration uses 4 quarter-turn direction groups (option "direction_groups")
+  int groups4_phys;  // the dts pre-pass does (options "direction_groups", "phys_groups")
   int adv_groups4;   // the propagation kernel does (options "direction_groups", "advect_groups")
+  // Launch configuration of the three spectral kernels, chosen by the
+  // autotuner or the options: the resident CTAs per SM their register budget
+  // is sized for (__launch_bounds__ instances) and how many frequency levels
+  // ahead they prefetch the spectrum and table rows into L2.  Results do not
+  // depend on these.
+  int minb_phys, minb_integ, minb_adv;
+  int pf_phys, pf_integ, pf_adv;
+  int count_cut;     // the propagation counts the bins its non-negativity cut changes (Global::cut_count)
   float f[MAX_OM], dom[MAX_OM];
   float th[MAX_PM], cth[MAX_PM], sth[MAX_PM], c2th[MAX_PM], s2th[MAX_PM];
   // max(cos th, 0), min(cos th, 0), max(sin th, 0), min(sin th, 0): the
@@ -115,6 +138,7 @@ struct Global {
   int iters;               // substeps the graph-driven inner loop ran since it was armed
   int nonfinite;           // non-finite values found by the last finite check
   int save_src;            // the last substep of this dtg keeps its source terms (for stress('ocn'))
+  unsigned long long cut_count;  // bins whose negative ef the propagation cut to 0 (option "count_cut")
 };
 
 struct Ptrs {

@@ -87,18 +87,6 @@ __device__ __forceinline__ float sin_fold(const Params& prm, float shelt, float 
   return s;
 }
 
-// levels ahead the kernels prefetch the spectrum (and table) rows into L2;
-// measured on 1000x1000: the integration and the propagation are fastest at
-// one level (two: +3 % and +5 %, four: +13 % and +8 %), the dts pre-pass at two
-#ifndef UMWM_PF_DIST_PHYS
-#define UMWM_PF_DIST_PHYS 2
-#endif
-#ifndef UMWM_PF_DIST_INTEG
-#define UMWM_PF_DIST_INTEG 1
-#endif
-#ifndef UMWM_PF_DIST_ADV
-#define UMWM_PF_DIST_ADV 1
-#endif
 #ifndef UMWM_PREFETCH_TAB
 #define UMWM_PREFETCH_TAB 1  // the spectral kernels also prefetch the block's table rows with the spectrum
 #endif

@@ -10,6 +10,8 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <functional>
 #include <cmath>
 #include <cstdio>
@@ -90,6 +92,45 @@ struct MemberHost {
   int substep_mark = 0;  // member substep counter at the start of the last run
 };
 
+// Online autotuner of the three spectral kernels' launch configuration.
+//
+// Each kernel (dts pre-pass, integration, propagation) has a candidate list
+// of (direction mapping, resident CTAs per SM, prefetch distance).  While the
+// tuner is active the inner loop runs host-driven and substep s launches each
+// kernel with its candidate s mod n (round-robin, `reps` times each), timed
+// with CUDA events on the model's stream; once a kernel has all its samples
+// it keeps the candidate with the smallest mean time.  The tuner measures the
+// model's real substeps, so tuning costs no extra work.  Register budgets and
+// prefetch distances do not change any result (mode 1); the direction mapping
+// changes the summation order of the partial sums (mode 2, results differ by
+// rounding: both mappings meet the parity bars).  Choices are cached per
+// domain signature for the life of the process.
+struct TuneCand {
+  int g4, minb, pf;  // quarter-turn groups, CTAs per SM (0: default instance), levels prefetched
+};
+struct KernelTune {
+  std::vector<TuneCand> cands;
+  std::vector<double> ms;
+  std::vector<int> n;
+  int best = -1;
+};
+enum { TK_PHYS = 0, TK_INTEG, TK_ADVECT, TK_N };
+struct Tuner {
+  int mode = 0;         // 0 off, 1 register budgets and prefetch, 2 also the direction mapping
+  bool active = false;  // measuring
+  bool done = false;    // a choice is in place (tuned or from the cache)
+  int reps = 2;
+  int step = 0;         // substeps measured so far
+  KernelTune k[TK_N];
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> kev;  // pending (kernel, events)
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  ~Tuner() {
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+  }
+};
+std::map<std::string, std::array<TuneCand, TK_N>> g_tune_cache;
+
 struct Model {
   std::vector<MemberHost> mem;
   bool on_device = false;
@@ -136,6 +177,7 @@ struct Model {
   double kms[K_NK] = {0};
   long long kcnt[K_NK] = {0};
   float *E = nullptr, *ES = nullptr, *TAB = nullptr;
+  Tuner tune;
 
   ~Model() {
     for (cudaEvent_t e : evpool) cudaEventDestroy(e);
@@ -188,6 +230,147 @@ void collect_timings(Model& M) {
   }
   M.kev.clear();
   M.evused = 0;
+}
+
+// ---- autotuner --------------------------------------------------------------
+void drop_graph(Model& M) {  // the captured inner loop holds the old launch configuration
+  if (M.graph_exec) { cudaGraphExecDestroy(M.graph_exec); M.graph_exec = nullptr; }
+  if (M.graph) { cudaGraphDestroy(M.graph); M.graph = nullptr; }
+}
+
+std::string tune_key(const Model& M) {
+  const Params& p = M.prm;
+  return std::to_string(p.ntiles) + "/" + std::to_string(p.O) + "/" + std::to_string(p.P) + "/" +
+         std::to_string(p.nmem) + "/" + std::to_string(p.curvilinear) + "/" + std::to_string(M.tune.mode);
+}
+
+// the launch configuration of kernel k in M.prm
+TuneCand tune_get(const Params& p, int k) {
+  if (k == TK_PHYS) return {p.groups4_phys, p.minb_phys, p.pf_phys};
+  if (k == TK_INTEG) return {p.groups4, p.minb_integ, p.pf_integ};
+  return {p.adv_groups4, p.minb_adv, p.pf_adv};
+}
+void tune_set(Params& p, int k, const TuneCand& c) {
+  if (k == TK_PHYS) { p.groups4_phys = c.g4; p.minb_phys = c.minb; p.pf_phys = c.pf; }
+  else if (k == TK_INTEG) { p.groups4 = c.g4; p.minb_integ = c.minb; p.pf_integ = c.pf; }
+  else { p.adv_groups4 = c.g4; p.minb_adv = c.minb; p.pf_adv = c.pf; }
+}
+
+// Candidate lists.  Register budgets have kernel instances only for the
+// 36-direction mappings (the integration's two-group shared memory allows at
+// most 4 CTAs; the propagation's tuned instances are for plain grids).
+void tune_start(Model& M, int mode) {
+  Tuner& T = M.tune;
+  T.mode = mode;
+  T.active = T.done = false;
+  T.step = 0;
+  if (mode == 0) return;
+  const Params& p = M.prm;
+  auto it = g_tune_cache.find(tune_key(M));
+  if (it != g_tune_cache.end()) {
+    for (int k = 0; k < TK_N; ++k) tune_set(M.prm, k, it->second[k]);
+    T.done = true;
+    drop_graph(M);
+    return;
+  }
+  const bool d36 = p.P == 36;
+  for (int k = 0; k < TK_N; ++k) {
+    KernelTune& K = T.k[k];
+    K.cands.clear();
+    const TuneCand cur = tune_get(p, k);
+    std::vector<int> g4s = {cur.g4};
+    if (mode == 2 && quarter_groups(p.P)) g4s = {0, 1};
+    for (int g4 : g4s) {
+      std::vector<int> minbs = {0}, pfs;
+      if (k == TK_PHYS) {
+        if (d36) minbs = g4 ? std::vector<int>{4, 5, 6} : std::vector<int>{5, 6, 7};
+        pfs = {1, 2, 3};
+      } else if (k == TK_INTEG) {
+        if (d36) minbs = g4 ? std::vector<int>{3, 4, 5} : std::vector<int>{3, 4};
+        pfs = {1, 2};
+      } else {
+        if (d36 && !p.curvilinear) minbs = {3, 4, 5};
+        pfs = {1, 2};
+      }
+      for (int mb : minbs)
+        for (int pf : pfs) K.cands.push_back({g4, mb, pf});
+    }
+    K.ms.assign(K.cands.size(), 0.0);
+    K.n.assign(K.cands.size(), 0);
+    K.best = -1;
+  }
+  T.active = true;
+  drop_graph(M);
+}
+
+// configuration of the next measured substep
+void tune_apply(Model& M) {
+  Tuner& T = M.tune;
+  for (int k = 0; k < TK_N; ++k) {
+    const KernelTune& K = T.k[k];
+    const int c = K.best >= 0 ? K.best : (int)(T.step % K.cands.size());
+    tune_set(M.prm, k, K.cands[c]);
+  }
+}
+
+cudaEvent_t tune_event(Tuner& T) {
+  if (T.used == T.pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    T.pool.push_back(e);
+  }
+  return T.pool[T.used++];
+}
+
+// after the substep's stream synchronisation: book its times
+void tune_collect(Model& M) {
+  Tuner& T = M.tune;
+  if (!T.active || T.kev.empty()) return;
+  for (auto& kv : T.kev) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, kv.second.first, kv.second.second) != cudaSuccess) continue;
+    KernelTune& K = T.k[kv.first];
+    if (K.best >= 0) continue;
+    const int c = (int)(T.step % K.cands.size());
+    K.ms[c] += ms;
+    K.n[c] += 1;
+  }
+  T.kev.clear();
+  T.used = 0;
+  T.step++;
+  bool all = true;
+  for (int k = 0; k < TK_N; ++k) {
+    KernelTune& K = T.k[k];
+    if (K.best >= 0) continue;
+    if (T.step < (int)K.cands.size() * T.reps) { all = false; continue; }
+    double bm = 1e300;
+    for (size_t c = 0; c < K.cands.size(); ++c)
+      if (K.n[c] > 0 && K.ms[c] / K.n[c] < bm) { bm = K.ms[c] / K.n[c]; K.best = (int)c; }
+    if (K.best < 0) K.best = 0;
+  }
+  if (!all) return;
+  std::array<TuneCand, TK_N> choice;
+  for (int k = 0; k < TK_N; ++k) {
+    choice[k] = T.k[k].cands[T.k[k].best];
+    tune_set(M.prm, k, choice[k]);
+  }
+  g_tune_cache[tune_key(M)] = choice;
+  T.active = false;
+  T.done = true;
+  drop_graph(M);
+}
+
+// Launch wrapper of the tuned kernels: events for the tuner while it
+// measures, else the kernel-timing wrapper.
+template <typename F>
+cudaError_t tuned(Model& M, int tk, int kname, F&& launch) {
+  if (!M.tune.active) return timed(M, kname, launch);
+  cudaEvent_t a = tune_event(M.tune), b = tune_event(M.tune);
+  cudaEventRecord(a, M.st);
+  cudaError_t e = launch();
+  cudaEventRecord(b, M.st);
+  M.tune.kev.push_back({tk, {a, b}});
+  return e;
 }
 
 // per-(o,i) tables in the blocked device layout [o][j/32][t][32], one member
@@ -387,6 +570,12 @@ int setup_params(Model& M) {
     p.s2th[q] = (float)std::sin(2.0 * (double)H.th[q]);
   }
   for (int l = 0; l < H.lm; ++l) p.depth[l] = H.depth[l];
+  // launch configuration: default register budgets (0) and prefetch distances
+  p.minb_phys = p.minb_integ = p.minb_adv = 0;
+  p.count_cut = 0;
+  p.pf_phys = UMWM_PF_DIST_PHYS;
+  p.pf_integ = UMWM_PF_DIST_INTEG;
+  p.pf_adv = UMWM_PF_DIST_ADV;
   return UMWM_OK;
 }
 
@@ -410,7 +599,8 @@ int init_device(Model& M) {
     int dev = 0, nsm = 0;
     CU(cudaGetDevice(&dev));
     CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    if (quarter_groups(p.P) && (long)p.ntiles < (long)UMWM_AUTO_G4_TILES * nsm) p.groups4 = p.adv_groups4 = 1;
+    if (quarter_groups(p.P) && (long)p.ntiles < (long)UMWM_AUTO_G4_TILES * nsm)
+      p.groups4 = p.groups4_phys = p.adv_groups4 = 1;
   }
   M.dev.reset(new Dev());
   Dev& D = *M.dev;
@@ -1098,7 +1288,7 @@ int enqueue_substep(Model& M, int compute_rot, int first, bool diag) {
   const Ptrs& P = M.P;
   CU(timed(M, K_PREP, [&] { return launch_prep(prm, P, compute_rot, M.max_nm, M.st); }));
   if (prm.ice_possible) CU(timed(M, K_SICE, [&] { return launch_sice(prm, P, M.st); }));
-  CU(timed(M, K_PHYS, [&] { return launch_source_phys(prm, P, compute_rot, M.st); }));
+  CU(tuned(M, TK_PHYS, K_PHYS, [&] { return launch_source_phys(prm, P, compute_rot, M.st); }));
   CU(timed(M, K_DTS, [&] { return launch_dts(prm, P, compute_rot, first, M.st); }));
   int rc;
   if (sur::active()) {
@@ -1109,10 +1299,10 @@ int enqueue_substep(Model& M, int compute_rot, int first, bool diag) {
     CU(timed(M, K_INTEG, [&] { return launch_source_integ(prm, fbP, M.st); }));
   } else {
     if (sur::capturing() && (rc = sur::capture_before(prm, P, M.wet_ranges, M.st))) return rc;
-    CU(timed(M, K_INTEG, [&] { return launch_source_integ(prm, P, M.st); }));
+    CU(tuned(M, TK_INTEG, K_INTEG, [&] { return launch_source_integ(prm, P, M.st); }));
     if (sur::capturing() && (rc = sur::capture_after(prm, P, M.st))) return rc;
   }
-  CU(timed(M, K_ADVECT, [&] { return launch_advect(prm, P, M.st); }));
+  CU(tuned(M, TK_ADVECT, K_ADVECT, [&] { return launch_advect(prm, P, M.st); }));
   if (diag) CU(timed(M, K_DIAG, [&] { return launch_diag(prm, P, M.st); }));
   CU(timed(M, K_SCREEN, [&] { return launch_screen(prm, P, M.st); }));
   return UMWM_OK;
@@ -1122,6 +1312,19 @@ int substep_launches(const Model& M, bool diag) { return 6 + (M.prm.ice_possible
 
 int substep(Model& M) {
   const bool first = M.first;
+  // the tuner measures from the second substep of the model on
+  if (M.tune.active && first) {
+    for (int k = 0; k < TK_N; ++k) tune_set(M.prm, k, M.tune.k[k].cands[0]);
+    M.tune.active = false;  // not measured: the first substep also runs diag
+    int rc = enqueue_substep(M, (M.prm.currents || first) ? 1 : 0, 1, true);
+    M.tune.active = true;
+    if (rc) return rc;
+    M.launches += substep_launches(M, true);
+    M.first = false;
+    M.substeps++;
+    return UMWM_OK;
+  }
+  if (M.tune.active) tune_apply(M);
   int rc = enqueue_substep(M, (M.prm.currents || first) ? 1 : 0, first ? 1 : 0, first);
   if (rc) return rc;
   M.launches += substep_launches(M, first);
@@ -1261,7 +1464,7 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     for (long long inner = 0;;) {
       if (inner > 10000000LL) return fail(UMWM_ERR_TIMEOUT, "umwm_run: more than 1e7 substeps in one dtg (dts stuck at 0?)");
       if (M.max_substeps >= 0 && M.substeps >= M.max_substeps) return finish_run(M);
-      if (M.use_graph && !M.first && !M.ktime && !sur::active() && !sur::capturing()) {
+      if (M.use_graph && !M.first && !M.ktime && !M.tune.active && !sur::active() && !sur::capturing()) {
         if ((rc = build_graph(M))) return rc;
         long long budget = GRAPH_CHUNK;
         if (M.max_substeps >= 0) budget = std::min(budget, M.max_substeps - M.substeps);
@@ -1291,6 +1494,7 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
       CU(cudaMemcpyAsync(M.flag_h, M.d_glob, sizeof(Global), cudaMemcpyDeviceToHost, M.st));
       CU(cudaStreamSynchronize(M.st));
       collect_timings(M);
+      tune_collect(M);
       if (M.flag_h->not_done == 0) break;
     }
     if (M.mem[0].H.stokes && M.prm.lm > 0) {
@@ -1903,15 +2107,44 @@ int umwm_gpu_set_option(const char* name, double value) {
     M->ocn_every = value != 0;
     return M->ocn_every ? ensure_ocn(*M) : UMWM_OK;
   }
-  if (s == "direction_groups" || s == "advect_groups") {
+  if (s == "direction_groups" || s == "advect_groups" || s == "phys_groups" || s == "integ_groups") {
     if (value != 2 && value != 4) return fail(UMWM_ERR_ARG, s + " must be 2 or 4");
     if (value == 4 && !quarter_groups(M->prm.P))
       return fail(UMWM_ERR_UNSUPPORTED, s + " 4 needs pm % 4 == 0 and pm/4 in {4, 6, 8, 9, 12}");
-    if (s == "direction_groups") M->prm.groups4 = value == 4 ? 1 : 0;
-    M->prm.adv_groups4 = value == 4 ? 1 : 0;
-    // the captured inner loop holds the old launch configuration
-    if (M->graph_exec) { cudaGraphExecDestroy(M->graph_exec); M->graph_exec = nullptr; }
-    if (M->graph) { cudaGraphDestroy(M->graph); M->graph = nullptr; }
+    const int g4 = value == 4 ? 1 : 0;
+    if (s == "direction_groups" || s == "integ_groups") M->prm.groups4 = g4;
+    if (s == "direction_groups" || s == "phys_groups") M->prm.groups4_phys = g4;
+    if (s == "direction_groups" || s == "advect_groups") M->prm.adv_groups4 = g4;
+    drop_graph(*M);
+    return UMWM_OK;
+  }
+  // launch configuration of the spectral kernels (what the autotuner sets):
+  // resident CTAs per SM of the register budget (0: the default instance; a
+  // budget without an instance also runs the default) and prefetch distance
+  {
+    int* f = s == "minb_phys" ? &M->prm.minb_phys : s == "minb_integ" ? &M->prm.minb_integ
+           : s == "minb_advect" ? &M->prm.minb_adv : s == "pf_phys" ? &M->prm.pf_phys
+           : s == "pf_integ" ? &M->prm.pf_integ : s == "pf_advect" ? &M->prm.pf_adv : nullptr;
+    if (f) {
+      if (value != std::floor(value) || value < 0 || value > 8)
+        return fail(UMWM_ERR_ARG, s + " must be an integer in [0, 8]");
+      *f = (int)value;
+      drop_graph(*M);
+      return UMWM_OK;
+    }
+  }
+  if (s == "count_cut") {
+    if (value != 0 && M->prm.P != 36)
+      return fail(UMWM_ERR_UNSUPPORTED, "count_cut needs pm = 36 (the counting kernel instances)");
+    M->prm.count_cut = value != 0 ? 1 : 0;
+    static const unsigned long long zero = 0;
+    CU(cudaMemcpy(&M->d_glob->cut_count, &zero, sizeof zero, cudaMemcpyHostToDevice));
+    drop_graph(*M);
+    return UMWM_OK;
+  }
+  if (s == "autotune") {
+    if (value != 0 && value != 1 && value != 2) return fail(UMWM_ERR_ARG, "autotune must be 0, 1 or 2");
+    tune_start(*M, (int)value);
     return UMWM_OK;
   }
   return fail(UMWM_ERR_ARG, "set_option: unknown option " + s);
@@ -1926,6 +2159,21 @@ double umwm_gpu_get_stat(const char* name) {
   if (s == "gpu_ms") return M->last_gpu_ms;
   if (s == "bin_updates") return M->last_bins;
   if (s == "launches") return (double)M->launches;
+  if (s == "cut_count") {  // bins the non-negativity cut changed since count_cut was set
+    unsigned long long c = 0;
+    if (cudaMemcpy(&c, &M->d_glob->cut_count, sizeof c, cudaMemcpyDeviceToHost) != cudaSuccess) return -1.0;
+    return (double)c;
+  }
+  if (s == "autotune_active") return M->tune.active ? 1.0 : 0.0;
+  if (s == "autotune_done") return M->tune.done ? 1.0 : 0.0;
+  if (s == "autotune_substeps") return (double)M->tune.step;
+  // launch configuration in use, encoded as direction groups (2 or 4) * 100
+  // + CTAs per SM * 10 + prefetch levels (CTAs 0: the default instance)
+  if (s == "config:phys" || s == "config:integ" || s == "config:advect") {
+    const int k = s == "config:phys" ? TK_PHYS : s == "config:integ" ? TK_INTEG : TK_ADVECT;
+    const TuneCand c = tune_get(M->prm, k);
+    return (c.g4 ? 4 : 2) * 100.0 + c.minb * 10.0 + c.pf;
+  }
   if (s == "device_free_bytes") {  // cudaMemGetInfo of the current device
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return -1.0;
