@@ -259,7 +259,8 @@ def run_ensemble(args):
     graph instantiation and, with --autotune, the tuner's measurements: three
     dtgs) and times the next dtg: the sequential arm member by member
     (initialize untimed), the batched arm as one ensemble.  Both arms run the
-    graph-driven inner loop with the same tuner mode.  The significant wave
+    graph-driven inner loop (or, with --persistent, the persistent substep
+    kernel) with the same tuner mode.  The significant wave
     height of every member after the timed dtg must be bit-identical between
     the arms (mode 1 tunes nothing that changes results)."""
     rank, world, local_rank = rank_info()
@@ -269,7 +270,7 @@ def run_ensemble(args):
     dtg = 600
     lo = tuple(int(x) for x in args.member_lo.split("x"))
     hi = tuple(int(x) for x in args.member_hi.split("x"))
-    nd = 5  # forcing for up to four untimed dtgs and the timed one
+    nd = 6  # forcing for the untimed dtgs and the timed one
     members = configs.ensemble_members(args.members, seed=11, size_lo=lo, size_hi=hi, hours=nd * dtg / 3600.0,
                                        dtg=dtg, warm=False)
     start = members[0].start
@@ -277,9 +278,9 @@ def run_ensemble(args):
     U.set_option("device", local_rank)
     wet = [c.meta["im"] for c in members]
 
-    # untimed dtgs: one, or three with the tuner (its 19 substeps need more
-    # than one 600 s dtg); both arms time the same dtg
-    nwarm = 3 if args.autotune else 1
+    # untimed dtgs: one, or four with the tuner (its 46 substeps need several
+    # 600 s dtgs); both arms time the same dtg
+    nwarm = 4 if args.autotune else 1
 
     def warm(tuned):
         for k in range(nwarm):
@@ -288,12 +289,14 @@ def run_ensemble(args):
 
     seq_ms = seq_bins = seq_sub = 0.0
     seq_ht = []
+    seq_groups = set()
     t_seq = time.perf_counter()
     for c in members:
         U.clear_inputs()
         c.stage(U)
         U.umwm_initialize(nml_text=c.nml)
         U.set_option("use_graph", 1)
+        U.set_option("persistent", 1 if args.persistent else 0)
         if args.autotune:
             U.set_option("autotune", args.autotune)
         k = warm(args.autotune)
@@ -303,6 +306,7 @@ def run_ensemble(args):
         seq_bins += U.stat("bin_updates")
         seq_sub += U.dims()["substeps"] - s0
         seq_ht.append((k, U.get_field("ht")))
+        seq_groups.add(int(U.stat("config:integ")) // 100)
         U.umwm_finalize()
     t_seq = time.perf_counter() - t_seq
 
@@ -314,10 +318,12 @@ def run_ensemble(args):
     U.ensemble_initialize()
     t_init = time.perf_counter() - t0
     U.set_option("use_graph", 1)
+    U.set_option("persistent", 1 if args.persistent else 0)
     if args.autotune:
         U.set_option("autotune", args.autotune)
     k = warm(args.autotune)
     tune = {kk: int(U.stat("config:" + kk)) for kk in ("phys", "integ", "advect")} if args.autotune else None
+    bat_groups = int(U.stat("config:integ")) // 100
     launches0 = U.stat("launches")
     clocks = Clocks(local_rank)
     clocks.start()
@@ -329,11 +335,21 @@ def run_ensemble(args):
     bat_outer = U.dims()["substeps"] - s0
     launches = int(U.stat("launches") - launches0)
     same = True
+    hs_diff = 0.0
     for m in range(len(members)):
         U.select_member(m)
         km, htm = seq_ht[m]
-        same = same and km == k and bool(np.array_equal(U.get_field("ht"), htm))
+        hb = U.get_field("ht")
+        same = same and km == k and bool(np.array_equal(hb, htm))
+        wm = htm > 1e-3
+        if wm.any():
+            hs_diff = max(hs_diff, float((np.abs(hb - htm)[wm] / htm[wm]).max()))
     U.umwm_finalize()
+    # members small enough to run alone with the quarter-turn direction
+    # mapping (chosen by size) round differently from the batch, which runs
+    # the half-turn mapping: then the arms agree to rounding, not bit for bit
+    if seq_groups != {bat_groups}:
+        same = None
 
     batched = bat_bins / (bat_ms / 1e3)
     sequential = seq_bins / (seq_ms / 1e3)
@@ -345,12 +361,14 @@ def run_ensemble(args):
                                    "timed" % (len(members), lo[0], lo[1], hi[0], hi[1], dtg, k + 1),
                        "members": len(members), "wet_points": int(sum(wet)), "wet_min": int(min(wet)),
                        "wet_max": int(max(wet)), "bins_per_point": BINS, "autotune": args.autotune,
+                       "persistent": bool(args.persistent),
                        "batched_config": tune},
             "batched": {"value": batched, "gpu_ms": bat_ms, "bin_updates": bat_bins, "init_s": t_init},
             "sequential": {"value": sequential, "gpu_ms": seq_ms, "bin_updates": seq_bins,
                            "member_substeps": seq_sub, "wall_s_incl_init": t_seq},
             "batched_over_sequential": batched / sequential,
             "bins_match": bool(bat_bins == seq_bins), "hs_bit_identical": same,
+            "hs_max_rel_diff": hs_diff, "direction_groups": {"sequential": sorted(seq_groups), "batched": bat_groups},
             "gpu_launches": launches, "clocks": clk,
             "timing": "CUDA events on the model's stream around umwm_gpu_run of the timed dtg (both arms)"}
     if rank == 0:
@@ -403,11 +421,24 @@ def run_surrogate(args):
         del case
     U.surrogate_capture(0, 0)
     t_gen = time.perf_counter() - t0
+    # training: the last 2 % of the pairs are held out; three phases of
+    # decreasing learning rate (half, a quarter, a quarter of the steps), the
+    # energy-weighted loss (bins at the EPS floor count little)
+    npairs = int(U.stat("surrogate_pairs"))
+    nhold = max(8192, npairs // 50)
+    U.set_option("surrogate_holdout", nhold)
+    U.set_option("surrogate_loss_weight", 1 if args.sur_weighted else 0)
+    held = [{"step": 0, "loss": U.surrogate_eval(npairs - nhold, nhold)}]
     t0 = time.perf_counter()
-    l1 = U.surrogate_train(args.train_steps, batch=8192, lr=1e-3, seed=1)
-    l2 = U.surrogate_train(args.train_steps // 2, batch=8192, lr=2e-4, seed=2)
+    parts = []
+    done_steps = 0
+    for frac, lr, seed in ((0.5, 1e-3, 1), (0.25, 3e-4, 2), (0.25, 1e-4, 3)):
+        n = max(1, int(args.train_steps * frac))
+        parts.append(U.surrogate_train(n, batch=8192, lr=lr, seed=seed))
+        done_steps += n
+        held.append({"step": done_steps, "lr": lr, "loss": U.surrogate_eval(npairs - nhold, nhold)})
     t_train = time.perf_counter() - t0
-    losses = np.concatenate([l1, l2])
+    losses = np.concatenate(parts)
 
     ev = configs.hurricane(mm=args.size, nm=args.size, hours=args.hours, seed=5)
 
@@ -481,6 +512,50 @@ def run_surrogate(args):
         dir_err = {"mean_abs_deg": float(_angle_err_deg(sur["mwd"], plain["mwd"])[wet].mean()),
                    "hs_weighted_deg": float((_angle_err_deg(sur["mwd"], plain["mwd"]) * hp)[wet].sum()
                                             / hp[wet].sum())}
+    # against the fp64 oracle: the same hurricane on a smaller grid, run with
+    # the plain path, the surrogate and the fp64 oracle
+    sur_fp64 = None
+    if args.sur_fp64_size > 0:
+        from oracle import pyoracle
+
+        small = configs.hurricane(mm=args.sur_fp64_size, nm=args.sur_fp64_size, hours=args.hours, seed=5)
+        fields = {}
+        for tag, use in (("plain", False), ("surrogate", True)):
+            U.clear_inputs()
+            small.stage(U)
+            U.umwm_initialize(nml_text=small.nml)
+            U.set_option("surrogate", 1 if use else 0)
+            p0, f0 = U.stat("surrogate_points"), U.stat("surrogate_fallback")
+            U.set_option("check_finite", 1)
+            try:
+                U.umwm_run(small.start, small.stop)
+                fields[tag] = {k: U.get_field(k).astype(np.float64) for k in ("ht", "dwp", "mwd")}
+                fields[tag]["fallback"] = (U.stat("surrogate_fallback") - f0) / max(U.stat("surrogate_points") - p0, 1)
+            except U.UmwmError as exc:
+                fields[tag] = {"error": str(exc)}
+            U.set_option("surrogate", 0)
+            U.umwm_finalize()
+        pyoracle.set_threads(os.cpu_count() or 1)
+        o = pyoracle.Oracle(small.nml, 64)
+        small.stage(o)
+        o.initialize()
+        o.run(small.start, small.stop)
+        ref = {k: np.asarray(o.get(k), dtype=np.float64) for k in ("ht", "dwp", "mwd")}
+        wet = ref["ht"] > 1e-3
+        sur_fp64 = {"case": "hurricane %dx%d dx=2km seed 5, %g h" % (args.sur_fp64_size, args.sur_fp64_size,
+                                                                      args.hours)}
+        for tag, f in fields.items():
+            if "error" in f:
+                sur_fp64[tag] = f
+                continue
+            rel = np.abs(f["ht"] - ref["ht"])[wet] / ref["ht"][wet]
+            sur_fp64[tag] = {"hs_max_rel": float(rel.max()), "hs_mean_rel": float(rel.mean()),
+                             "hs_p99_rel": float(np.percentile(rel, 99)),
+                             "tp_mean_rel": float((np.abs(f["dwp"] - ref["dwp"])[wet] / ref["dwp"][wet]).mean()),
+                             "tp_same_bin_frac": float((np.abs(f["dwp"] - ref["dwp"]) <= 1e-5 * ref["dwp"])[wet].mean()),
+                             "dir_mean_abs_deg": float(_angle_err_deg(f["mwd"], ref["mwd"])[wet].mean()),
+                             "fallback_fraction": float(f["fallback"])}
+        del o
     v_sur = sur["bins"] / (sur["gpu_ms"] / 1e3) if sur["gpu_ms"] > 0 else 0.0
     v_plain = plain["bins"] / (plain["gpu_ms"] / 1e3)
     flops_row = 2.0 * (1344 * 512 + 512 * 512 + 512 * 1344)
@@ -502,7 +577,10 @@ def run_surrogate(args):
             "hs_error_vs_plain": hs_err, "tp_error_vs_plain": tp_err, "dir_error_vs_plain": dir_err,
             "hs_error_vs_plain_hourly": hourly_err, "surrogate_run_stopped": sur["stopped"],
             "nonfinite_points_end": int((~np.isfinite(hs)).sum()),
-            "train": {"seconds": t_train, "loss_first": float(losses[:20].mean()), "loss_last": float(losses[-20:].mean())},
+            "train": {"seconds": t_train, "steps": int(len(losses)), "weighted_loss": bool(args.sur_weighted),
+                      "loss_first": float(losses[:20].mean()), "loss_last": float(losses[-20:].mean()),
+                      "heldout_pairs": nhold, "heldout_loss": held},
+            "vs_fp64": sur_fp64,
             "generate_seconds": t_gen,
             "surrogate_ms_per_step": {"features": sur["ms_features"] / max(sur["timed_steps"], 1),
                                       "gemm": sur["ms_gemm"] / max(sur["timed_steps"], 1),
@@ -663,11 +741,16 @@ def main():
     ap.add_argument("--acc-hurricane-hours", type=float, default=3.0)
     ap.add_argument("--pairs", type=int, default=2000000)
     ap.add_argument("--pts-per-substep", type=int, default=16384)
-    ap.add_argument("--train-steps", type=int, default=2000)
+    ap.add_argument("--train-steps", type=int, default=120000, help="Adam steps of the surrogate (three phases)")
+    ap.add_argument("--sur-weighted", type=int, default=1, help="energy-weighted surrogate loss")
+    ap.add_argument("--sur-fp64-size", type=int, default=120,
+                    help="grid of the surrogate's comparison with the fp64 oracle (0: none)")
     ap.add_argument("--hours", type=float, default=12.0)
     ap.add_argument("--sur-tol", type=float, default=0.02, help="surrogate total-energy budget per substep")
     ap.add_argument("--sur-tol-level", type=float, default=0.1, help="surrogate per-level energy budget")
     ap.add_argument("--members", type=int, default=64)
+    ap.add_argument("--persistent", action="store_true",
+                    help="ensemble arms run the inner loop as the persistent substep kernel")
     ap.add_argument("--member-lo", default="200x200", help="smallest ensemble member grid, MMxNM")
     ap.add_argument("--member-hi", default="1000x600", help="largest ensemble member grid, MMxNM")
     ap.add_argument("--autotune", type=int, default=1, choices=[0, 1, 2],
@@ -732,7 +815,9 @@ def main():
         cfg = {k: int(U.stat("config:" + k)) for k in ("phys", "integ", "advect")}
         tune = {"mode": args.autotune, "substeps_measured": int(U.stat("autotune_substeps")),
                 "choice": {k: {"direction_groups": v // 100, "ctas_per_sm": (v // 10) % 10 or "default",
-                               "prefetch_levels": v % 10} for k, v in cfg.items()}}
+                               "prefetch_levels": v % 10} for k, v in cfg.items()},
+                "median_ms": {k: {str(int(U.stat("tune_cfg:%s:%d" % (k, i)))): round(U.stat("tune_ms:%s:%d" % (k, i)), 4)
+                                  for i in range(int(U.stat("tune_n:" + k)))} for k in cfg}}
     case.restart = None  # drop the host copies of the 4.3 GB restart spectrum
     U.clear_inputs()
     for t, vars_ in case.forcing.items():

@@ -11,7 +11,9 @@ kernels can be checked against it:
                          hidden activations, f32 accumulation, f32 output,
                          bf16 output gradient and bf16 back-propagated
                          activation gradients, pre-activations kept in bf16;
-  * loss                 mean squared error over the first om*pm columns.
+  * loss                 mean squared error over the first om*pm columns,
+                         optionally weighted per bin by energy_weight of
+                         its input feature (the GPU's "surrogate_loss_weight").
 
 It is never part of the product path.
 """
@@ -24,6 +26,14 @@ NEXTRA = 9
 EPS = 1e-15
 LN_C0, LN_C1 = -15.0, 8.0
 TS = 2.0
+WL0, WL1, WMIN = -20.7232658, -11.5129255, 0.01  # ln 1e-9, ln 1e-5, floor
+
+
+def energy_weight(x):
+    """Weight of a target bin from its input feature x = (ln(e + EPS) - LN_C0)
+    / LN_C1: a ramp in ln e from WL0 (weight WMIN) to WL1 (weight 1)."""
+    w = (np.asarray(x, dtype=np.float32) * np.float32(LN_C1) + np.float32(LN_C0) - np.float32(WL0)) / np.float32(WL1 - WL0)
+    return np.clip(w, np.float32(WMIN), np.float32(1.0)).astype(np.float32)
 
 OFF_W1 = 0
 OFF_B1 = OFF_W1 + HID * FPAD
@@ -81,15 +91,23 @@ def forward(w, X):
     return Y, dict(Xb=Xb, Z1=bf16(Z1), H1=H1, Z2=bf16(Z2), H2=H2)
 
 
-def loss_and_grad(w, X, T, f0):
+def _weights(X, f0, weighted, dtype):
+    W = np.ones(X.shape, dtype=dtype)
+    if weighted:
+        W[:, :f0] = energy_weight(bf16(X)[:, :f0])
+    return W
+
+
+def loss_and_grad(w, X, T, f0, weighted=False):
     """Loss and gradient (packed like the parameters) of one batch."""
     W1, b1, W2, b2, W3, b3 = unpack(w)
     n = X.shape[0]
     Y, c = forward(w, X)
     d = np.zeros_like(Y)
     d[:, :f0] = Y[:, :f0] - bf16(T)[:, :f0]
-    loss = float((d.astype(np.float64) ** 2).sum() / (n * f0))
-    dY = bf16(2.0 * d / (n * f0))
+    Wt = _weights(X, f0, weighted, np.float32)
+    loss = float((Wt.astype(np.float64) * d.astype(np.float64) ** 2).sum() / (n * f0))
+    dY = bf16(np.float32(2.0) * (Wt * d) / np.float32(n * f0))
     gW3 = _mm(dY.T, c["H2"])
     gb3 = dY.sum(0, dtype=np.float64).astype(np.float32)
     dZ2 = bf16(_mm(dY, bf16(W3)) * gelu_grad(c["Z2"]))
@@ -101,7 +119,7 @@ def loss_and_grad(w, X, T, f0):
     return loss, pack(gW1, gb1, gW2, gb2, gW3, gb3)
 
 
-def loss_and_grad_exact(w, X, T, f0):
+def loss_and_grad_exact(w, X, T, f0, weighted=False):
     """Same network in float64 without any rounding (for finite differences)."""
     W1, b1, W2, b2, W3, b3 = (a.astype(np.float64) for a in unpack(w))
     X = X.astype(np.float64)
@@ -114,8 +132,9 @@ def loss_and_grad_exact(w, X, T, f0):
     Y = H2 @ W3.T + b3
     d = np.zeros_like(Y)
     d[:, :f0] = Y[:, :f0] - T[:, :f0]
-    loss = (d ** 2).sum() / (n * f0)
-    dY = 2.0 * d / (n * f0)
+    Wt = _weights(X, f0, weighted, np.float64)
+    loss = (Wt * d ** 2).sum() / (n * f0)
+    dY = 2.0 * Wt * d / (n * f0)
     gW3 = dY.T @ H2
     dZ2 = (dY @ W3) * gelu_grad(Z2)
     gW2 = dZ2.T @ H1

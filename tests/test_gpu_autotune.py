@@ -3,7 +3,7 @@
 
 Mode 1 tunes the register budget (resident CTAs per SM) and the L2 prefetch
 distance of the dts pre-pass, the integration and the propagation while the
-model's own substeps run, round-robin over the candidates.  Neither knob
+model's own substeps run, round-robin over the candidates, five samples each.  Neither knob
 changes any arithmetic, so a tuned run is compared bit for bit with an untuned
 one, also across the substeps during which the candidates rotate.  Mode 2
 also tunes the direction mapping, which changes summation order only: its run
@@ -40,16 +40,16 @@ def test_autotune_bit_identical(lib_built):
 
     U = lib_built
     case = configs.random_field(mm=64, nm=56, hours=1, dx=2000.0)
-    F0, u0, _ = _run(U, case, 0, 24)
-    F1, u1, info = _run(U, case, 1, 24)
+    F0, u0, _ = _run(U, case, 0, 50)
+    F1, u1, info = _run(U, case, 1, 50)
     np.testing.assert_array_equal(F1, F0)
     np.testing.assert_array_equal(u1, u0)
-    # 9 pre-pass candidates x 2 samples after the first substep: tuning done
-    assert info["done"] == 1 and info["active"] == 0 and info["measured"] == 18
+    # 9 pre-pass candidates x 5 samples after the first substep: tuning done
+    assert info["done"] == 1 and info["active"] == 0 and info["measured"] == 45
     for c in info["config"]:
         assert int(c) // 100 in (2, 4) and 1 <= int(c) % 10 <= 3
     # the same shape again starts from the cached choice
-    F2, u2, info2 = _run(U, case, 1, 24)
+    F2, u2, info2 = _run(U, case, 1, 50)
     assert info2["done"] == 1 and info2["measured"] == 0 and info2["config"] == info["config"]
     np.testing.assert_array_equal(F2, F0)
 
@@ -58,10 +58,10 @@ def test_autotune_direction_mapping_parity(lib_built, oracle_mod):
     from umwm_gb300 import configs
 
     U = lib_built
-    case = configs.random_field(mm=48, nm=40, hours=1, dx=2000.0)
-    # 18 pre-pass candidates (two mappings) x 2 samples after the first substep
-    F, _, info = _run(U, case, 2, 40)
-    assert info["done"] == 1 and info["measured"] == 36
-    o = run_oracle(oracle_mod, case, 32, max_substeps=40)
+    case = configs.random_field(mm=48, nm=40, hours=2, dx=2000.0)
+    # 18 pre-pass candidates (two mappings) x 5 samples after the first substep
+    F, _, info = _run(U, case, 2, 95)
+    assert info["done"] == 1 and info["measured"] == 90
+    o = run_oracle(oracle_mod, case, 32, max_substeps=95)
     l2, p999, _ = spec_stats(F, o.get("e"))
     assert l2 < 1e-4 and p999 < 1e-3, (l2, p999)

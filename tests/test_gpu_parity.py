@@ -344,3 +344,38 @@ def test_global_domain(U, oracle_mod, groups):
     assert np.array_equal(U.get_field_i("oc"), o.get("oc").astype(np.int32))
     _compare_state(U, o, 1e-4, 1e-3, vectors=VECTORS, o64=o64)
     U.umwm_finalize()
+
+
+def test_count_cut(U, oracle_mod):
+    """Option count_cut counts the bins whose negative ef the propagation cuts
+    to 0 before e = ef (the one deliberate deviation from the reference,
+    umwm_top.F90:113), without changing any result.  On the fetch-limited
+    wind sea neither the GPU nor the oracle cuts a bin; on the 2 km hurricane
+    the cut fires on at most a few bins per million bin-updates."""
+    from umwm_gb300 import configs
+
+    def run(case, count):
+        U.clear_inputs()
+        case.stage(U)
+        U.umwm_initialize(nml_text=case.nml)
+        if count:
+            U.set_option("count_cut", 1)
+        U.umwm_run(case.start, case.stop)
+        F, _ = U.get_state()
+        c = U.stat("cut_count") if count else None
+        subs = U.dims()["substeps"]
+        U.umwm_finalize()
+        return F, c, subs
+
+    fl = configs.fetch_limited(mm=40, nm=30, hours=2)
+    F1, c1, _ = run(fl, True)
+    F0, _, _ = run(fl, False)
+    np.testing.assert_array_equal(F1, F0)
+    assert c1 == 0
+    o = run_oracle(oracle_mod, fl, 32)
+    assert o.scalar("cut_count") == 0
+    hu = configs.hurricane(mm=100, nm=100, hours=2, dx=2000.0, dtg=600)
+    F1, c1, subs = run(hu, True)
+    F0, _, _ = run(hu, False)
+    np.testing.assert_array_equal(F1, F0)
+    assert 0 <= c1 <= 1e-6 * F0.size * subs, c1

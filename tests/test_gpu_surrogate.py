@@ -61,15 +61,18 @@ def test_forward_matches_oracle(lib_built, mo):
     assert np.abs(Y - Yo).max() < 2e-2 * np.abs(Yo).max()
 
 
-def test_gradient_matches_oracle(lib_built, mo):
+@pytest.mark.parametrize("weighted", [False, True])
+def test_gradient_matches_oracle(lib_built, mo, weighted):
     U = lib_built
     U.surrogate_init(37, 36, seed=7)
+    U.set_option("surrogate_loss_weight", 1 if weighted else 0)
     w = U.surrogate_get_params()
     w[mo.OFF_W3:mo.OFF_B3] *= 10.0
     U.surrogate_set_params(w)
     X, T = _batch(mo, 256, 2)
     loss, g = U.surrogate_grad(X, T)
-    lo, go = mo.loss_and_grad(w, X, T, 1332)
+    U.set_option("surrogate_loss_weight", 0)
+    lo, go = mo.loss_and_grad(w, X, T, 1332, weighted)
     assert abs(loss - lo) <= 1e-3 * lo
     for name, a, b in (("W1", mo.OFF_W1, mo.OFF_B1), ("b1", mo.OFF_B1, mo.OFF_W2), ("W2", mo.OFF_W2, mo.OFF_B2),
                        ("b2", mo.OFF_B2, mo.OFF_W3), ("W3", mo.OFF_W3, mo.OFF_B3), ("b3", mo.OFF_B3, mo.NPARAM)):

@@ -1,7 +1,9 @@
 """CPU checks of the surrogate's oracle (oracle/mlp_oracle.py): its exact
 backward pass against central finite differences, its bf16-rounded pass
-against the exact one, the bf16 rounding itself, and the feature rotation."""
+against the exact one (plain and energy-weighted loss), the bf16 rounding
+itself, the energy weight and the feature rotation."""
 import numpy as np
+import pytest
 
 from oracle import mlp_oracle as mo
 
@@ -25,17 +27,18 @@ def _batch(n, seed):
     return X, T
 
 
-def test_exact_gradient_vs_finite_differences():
+@pytest.mark.parametrize("weighted", [False, True])
+def test_exact_gradient_vs_finite_differences(weighted):
     w = _params(0).astype(np.float64)
     X, T = _batch(8, 1)
-    _, g = mo.loss_and_grad_exact(w, X, T, 1332)
+    _, g = mo.loss_and_grad_exact(w, X, T, 1332, weighted)
     rng = np.random.default_rng(2)
     idx = np.concatenate([rng.integers(a, b, 4) for a, b in ((mo.OFF_W1, mo.OFF_B1), (mo.OFF_B1, mo.OFF_W2),
                                                              (mo.OFF_W2, mo.OFF_B2), (mo.OFF_B2, mo.OFF_W3),
                                                              (mo.OFF_W3, mo.OFF_B3), (mo.OFF_B3, mo.OFF_B3 + 1332))])
 
     def loss(v):
-        return mo.loss_and_grad_exact(v, X, T, 1332)[0]
+        return mo.loss_and_grad_exact(v, X, T, 1332, weighted)[0]
 
     h = 1e-4
     for i in idx:
@@ -46,11 +49,12 @@ def test_exact_gradient_vs_finite_differences():
         assert abs(fd - g[i]) <= 1e-6 + 1e-4 * abs(g[i]), (i, fd, g[i])
 
 
-def test_rounded_gradient_close_to_exact():
+@pytest.mark.parametrize("weighted", [False, True])
+def test_rounded_gradient_close_to_exact(weighted):
     w = _params(3, scale3=10.0)
     X, T = _batch(64, 4)
-    l1, g1 = mo.loss_and_grad(w, X, T, 1332)
-    l2, g2 = mo.loss_and_grad_exact(w, mo.bf16(X), mo.bf16(T), 1332)
+    l1, g1 = mo.loss_and_grad(w, X, T, 1332, weighted)
+    l2, g2 = mo.loss_and_grad_exact(w, mo.bf16(X), mo.bf16(T), 1332, weighted)
     assert abs(l1 - l2) < 2e-2 * l2
     assert np.linalg.norm(g1 - g2) < 5e-2 * np.linalg.norm(g2)
 
@@ -77,3 +81,12 @@ def test_feature_rotation():
     k = 3 * pm + 0
     assert abs(X[0, k] - (np.log(1.0 + 1e-15) + 15.0) / 8.0) < 1e-6
     assert abs(X[0, 1332 + 1]) < 1e-6  # wind exactly on a bin: no offset
+
+
+def test_energy_weight_ramp():
+    # input features of bins at e = 1e-12, 1e-9, 1e-7, 1e-5, 1
+    e = np.array([1e-12, 1e-9, 1e-7, 1e-5, 1.0])
+    x = (np.log(e + mo.EPS) - mo.LN_C0) / mo.LN_C1
+    w = mo.energy_weight(x)
+    assert w[0] == np.float32(mo.WMIN) and abs(w[1] - mo.WMIN) < 1e-5
+    assert abs(w[2] - 0.5) < 1e-4 and w[3] == pytest.approx(1.0, abs=1e-5) and w[4] == 1.0

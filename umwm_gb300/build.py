@@ -17,7 +17,8 @@ LIB = os.path.join(OUT_DIR, "libumwm_gb300.so")
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["k_source.cu", "k_advect.cu", "k_misc.cu", "umwm_gpu.cu", "k_mlp.cu", "k_sur.cu", "surrogate.cu"]
+CU_SOURCES = ["k_source.cu", "k_advect.cu", "k_misc.cu", "k_persist.cu", "umwm_gpu.cu", "k_mlp.cu", "k_sur.cu",
+              "surrogate.cu"]
 CXX_SOURCES = ["host_model.cpp", "ncfile.cpp"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-ftz=true", "-Xcompiler", "-fPIC,-ffp-contract=off",
                      "-Xptxas", "-warn-spills"]

@@ -77,8 +77,11 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
   auto& scs = sm.scs;
   auto& stg = sm.stg;
   constexpr bool ST = AdvSmem<G, H, CURV>::ST;
-  // loads of E*: read-only path, or coherent in a persistent kernel
-  auto lde = [](const float* p) { return COH ? *p : __ldg(p); };
+  // loads of E*: the read-only path, or in a persistent kernel (which wrote
+  // E* in the same launch) loads cached in L2 only (ld.global.cg), which
+  // see the other CTAs' writes after the grid barrier.  E* is never written
+  // by this body, so its loads may be ordered freely against the e stores
+  auto lde = [](const float* __restrict__ p) { return COH ? __ldcg(p) : __ldg(p); };
 
   const float dta = ctl->dta, dtr = ctl->dtr;
   const bool zerocur = ctl->zerocurrents != 0;
@@ -182,7 +185,7 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
   // copies of level o's east/west rows (the cos slots A, B)
   auto stage = [&](int o) {
     if (ST && o < O && o < oc) {
-      const float* ESo = P.ES + (size_t)o * lstride;
+      const float* __restrict__ ESo = P.ES + (size_t)o * lstride;
 #pragma unroll
       for (int k = 0; k < (ST ? H : 0); ++k) {
         cp_async4(&stg[0][ST ? k : 0][threadIdx.x], ESo + oCA + k * 32);
@@ -205,7 +208,7 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
     if (ST) cp_async_wait<0>();  // this level's copies have landed
     constexpr int HH = HV ? H / NPART : 1;
     const float* T = P.TAB + (size_t)o * tstride;
-    const float* ESo = P.ES + (size_t)o * lstride;
+    const float* __restrict__ ESo = P.ES + (size_t)o * lstride;
     const float* EFo = P.EF + (size_t)o * lstride;
     float* Eo = P.E + (size_t)o * lstride;
     const bool prog = o < oc;
@@ -313,7 +316,7 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
     pf(o + PFD);
     if (ST) cp_async_wait<0>();  // this level's copies have landed
     const float* T = P.TAB + (size_t)o * tstride;
-    const float* ESo = P.ES + (size_t)o * lstride;
+    const float* __restrict__ ESo = P.ES + (size_t)o * lstride;
     const float* EFo = P.EF + (size_t)o * lstride;
     float* Eo = P.E + (size_t)o * lstride;
     float ef[H];

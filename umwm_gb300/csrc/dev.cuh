@@ -139,6 +139,10 @@ struct Global {
   int nonfinite;           // non-finite values found by the last finite check
   int save_src;            // the last substep of this dtg keeps its source terms (for stress('ocn'))
   unsigned long long cut_count;  // bins whose negative ef the propagation cut to 0 (option "count_cut")
+  // grid barrier of the persistent substep kernel: arrivals, generation,
+  // and the error flag a timed-out wait sets (reset before each launch)
+  unsigned bar_count, bar_gen;
+  int bar_err;
 };
 
 struct Ptrs {

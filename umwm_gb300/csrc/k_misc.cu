@@ -4,8 +4,8 @@
 #include <algorithm>
 #include <cfloat>
 
-#include "dev_common.cuh"
 #include "kernels.hpp"
+#include "misc_body.cuh"
 
 namespace umwm {
 
@@ -18,105 +18,22 @@ __global__ void k_prep(const Params prm, const Ptrs P, int compute_rot) {
   const Member& M = prm.mem[blockIdx.y];
   Ctl* ctl = M.ctl;
   if (ctl->done) return;
-  const float sumt = ctl->sumt, dtg = prm.dtg;
-  const float a = 1.f - sumt / dtg;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.NM; i += gridDim.x * blockDim.x) {
-    const int q = (M.mi[i] - 1) + (M.ni[i] - 1) * M.mm;
-    const int ia = M.nmoff + i;
-    if (prm.winds) {
-      float uw = M.uwb[q] * a + M.uwf[q] * sumt / dtg;
-      float vw = M.vwb[q] * a + M.vwf[q] * sumt / dtg;
-      if (prm.gustiness > 0.f) {  // umwm_forcing.F90:49-61
-        const float gu = prm.gustiness * (2.f * gust_uniform(prm.gust_seed, ctl->substep, q, 0) - 1.f);
-        const float gv = prm.gustiness * (2.f * gust_uniform(prm.gust_seed, ctl->substep, q, 1) - 1.f);
-        uw = uw * (1.f + gu);
-        vw = vw * (1.f + gv);
-      }
-      P.wspd[ia] = sqrtf(uw * uw + vw * vw);
-      P.wdir[ia] = atan2f(vw, uw);
-    }
-    if (prm.seaice) P.fice[ia] = M.ficeb[q] * a + M.ficef[q] * sumt / dtg;
-    if (prm.currents) {
-      P.uc[ia] = M.ucb[q] * a + M.ucf[q] * sumt / dtg;
-      P.vc[ia] = M.vcb[q] * a + M.vcf[q] * sumt / dtg;
-    }
-    if (prm.air_density) P.rhoa[ia] = M.rhoab[q] * a + M.rhoaf[q] * sumt / dtg;
-    if (prm.water_density) P.rhow[ia] = M.rhowb[q] * a + M.rhowf[q] * sumt / dtg;
-    P.rhorat[ia] = P.rhoa[ia] / P.rhow[ia];
-    const float ws = fmaxf(P.wspd[ia], 1e-2f);
-    P.wspd[ia] = ws;
-    if ((prm.isglobal || i < M.N) && (P.uc[ia] != 0.f || P.vc[ia] != 0.f)) ctl->anycurrent = 1;
-    if (i < M.N) {
-      const int j = M.off + i;
-      float fc = 0.53f * prm.g / ws;
-      if (fc > prm.fprog) fc = prm.fprog;
-      P.fcutoff[j] = fc;
-      int oc = 1;
-      for (int o = prm.O - 2; o >= 1; --o) {
-        oc = o;
-        if (fc > prm.f[o - 1]) break;
-      }
-      P.oc[j] = oc;
-      if (compute_rot) P.oc_rot[j] = oc;
-      P.shelt[j] = shelter_coare35(ws);
-    }
-  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.NM; i += gridDim.x * blockDim.x)
+    prep_point(prm, P, M, ctl, i, compute_rot);
 }
 
 // source(): dts = min(min_i physics_time_step, dtamin, dtg - sumt), the
 // first-step rule and sumt update (umwm_physics.F90:41-58); refraction's
 // dtr (umwm_advection.F90:145-158).  One thread.
 __global__ void k_dts(const Params prm, const Ptrs P, int compute_rot, int first) {
-  int left = 0;
-  for (int m = threadIdx.x; m < prm.nmem; m += blockDim.x) {
-    const Member& M = prm.mem[m];
-    Ctl& c = *M.ctl;
-    if (c.done) {  // finished this dtg in an earlier substep
-      c.running = 0;
-      continue;
-    }
-    float mn = dec_ord_d(c.minphys_enc);
-    float dts = fminf(fminf(mn, M.dtamin), prm.dtg - c.sumt);
-    if (!prm.restart && first) dts = 0.f;
-    c.dts = dts;
-    c.dta = dts;
-    c.sumt = c.sumt + dts;
-    if (compute_rot) {
-      float mx = dec_ord_d(c.maxrot_enc);
-      c.dtr_temp = (mx <= FLT_MIN) ? dts : prm.dth / mx;
-    }
-    c.dtr = fminf(c.dtr_temp, dts);
-    c.zerocurrents = c.anycurrent ? 0 : 1;
-    c.anycurrent = 0;
-    c.minphys_enc = enc_ord_d(__int_as_float(0x7f800000));
-    c.maxrot_enc = enc_ord_d(0.f);
-    c.done = (c.sumt < prm.dtg) ? 0 : 1;
-    c.running = 1;
-    c.first = first;
-    left += !c.done;
-  }
-  left = __syncthreads_count(left > 0) ? 1 : 0;  // any member left in this block
-  if (threadIdx.x == 0) P.glob->not_done = left;
+  dts_body(prm, P, compute_rot, first);
 }
 
 // s_ice: significant wave height where fice > fice_lth and the attenuation
 // factor C1*Hs (Hs < 3 m) or C1*3 (umwm_source_functions.F90:108-153).
 __global__ void k_sice(const Params prm, const Ptrs P) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= prm.Ntot) return;
-  const Member& M = prm.mem[prm.tile_mem[j / TILE]];
-  if (j >= M.ghost || M.ctl->done) return;
-  float sv = 0.f;
-  if (P.fice[apt(M, j)] > prm.fice_lth) {
-    float h = 0.f;
-    for (int p = 0; p < prm.P; ++p)
-      for (int o = 0; o < prm.O; ++o)
-        h += P.E[sidx(prm, o, p, j)] * P.TAB[tidx(prm, o, T_KDK, j)];
-    h = 4.f * sqrtf(h * prm.dth);
-    const float C1 = -5.35e-6f;
-    sv = (h < 3.f) ? C1 * h : C1 * 3.f;
-  }
-  P.sice_v[j] = sv;
+  if (j < prm.Ntot) sice_point(prm, P, j);
 }
 
 // diag, umwm_physics.F90:89-205, one thread per wet point.  The bins are
@@ -264,44 +181,7 @@ __global__ void k_stokes(const Params prm, const Ptrs P) {
 // also clears 'first' after the first substep.
 __global__ void k_screen(const Params prm, const Ptrs P) {
   __shared__ float s0[256], s2[256];
-  const Member& M = prm.mem[blockIdx.x];
-  Ctl& c = *M.ctl;
-  if (!c.running) return;
-  const int j = M.iip;
-  float a = 0.f, b = 0.f;
-  if (j >= 0) {
-    for (int b_ = threadIdx.x; b_ < prm.O * prm.P; b_ += blockDim.x) {
-      const int o = b_ / prm.P, p = b_ % prm.P;
-      const float ek = P.E[sidx(prm, o, p, j)] * P.TAB[tidx(prm, o, T_KDK, j)];
-      a += ek;
-      b += (prm.f[o] * prm.f[o]) * ek;
-    }
-  }
-  s0[threadIdx.x] = a;
-  s2[threadIdx.x] = b;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) { s0[threadIdx.x] += s0[threadIdx.x + s]; s2[threadIdx.x] += s2[threadIdx.x + s]; }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    const int r = c.log_count;
-    if (r < M.log_cap && j >= 0) {
-      double* L = M.log + (size_t)r * 8;
-      const int ja = apt(M, j);
-      L[0] = c.sumt / prm.dtg;
-      L[1] = c.dts;
-      L[2] = P.wspd[ja];
-      L[3] = P.wdir[ja];
-      L[4] = 4.f * sqrtf(s0[0] * prm.dth);
-      L[5] = sqrtf(s0[0] / s2[0]);
-      L[6] = P.cd[j] * 1e3f;
-      L[7] = prm.f[P.oc[j] - 1];
-      c.log_count = r + 1;
-    }
-    c.substep += 1;
-    c.first = 0;
-  }
+  screen_member<256, 256>(prm, P, blockIdx.x, s0, s2);
 }
 
 // Reference order F(om,pm,im) (o fastest) <-> the blocked device layout.

@@ -299,7 +299,8 @@ __global__ void k_transpose(const __nv_bfloat16* src, int rows, int cols, __nv_b
   }
 }
 
-__global__ void k_loss(const float* Y, const __nv_bfloat16* T, int n, int f0, __nv_bfloat16* dY, float* loss) {
+__global__ void k_loss(const float* Y, const __nv_bfloat16* T, const __nv_bfloat16* X, int n, int f0,
+                       __nv_bfloat16* dY, float* loss) {
   __shared__ float red[256];
   const size_t total = (size_t)n * FPAD;
   const float inv = 1.f / ((float)n * f0);
@@ -307,8 +308,9 @@ __global__ void k_loss(const float* Y, const __nv_bfloat16* T, int n, int f0, __
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
     const int c = static_cast<int>(i % FPAD);
     const float d = c < f0 ? Y[i] - __bfloat162float(T[i]) : 0.f;
-    acc += d * d;
-    dY[i] = __float2bfloat16_rn(2.f * d * inv);
+    const float w = (X && c < f0) ? energy_weight(__bfloat162float(X[i])) : 1.f;
+    acc += w * (d * d);
+    dY[i] = __float2bfloat16_rn(2.f * (w * d) * inv);
   }
   red[threadIdx.x] = acc;
   __syncthreads();
@@ -400,9 +402,9 @@ cudaError_t launch_transpose(const __nv_bfloat16* src, int rows, int cols, __nv_
   return cudaGetLastError();
 }
 
-cudaError_t launch_loss(const float* Y, const __nv_bfloat16* T, int n, int f0, __nv_bfloat16* dY, float* loss,
-                        cudaStream_t st) {
-  k_loss<<<grid_for((size_t)n * FPAD, 256), 256, 0, st>>>(Y, T, n, f0, dY, loss);
+cudaError_t launch_loss(const float* Y, const __nv_bfloat16* T, const __nv_bfloat16* X, int n, int f0,
+                        __nv_bfloat16* dY, float* loss, cudaStream_t st) {
+  k_loss<<<grid_for((size_t)n * FPAD, 256), 256, 0, st>>>(Y, T, X, n, f0, dY, loss);
   return cudaGetLastError();
 }
 

@@ -24,5 +24,12 @@ cudaError_t launch_loop_arm(Global* g, int budget, cudaStream_t st);
 cudaError_t launch_loop_cond(Global* g, cudaGraphConditionalHandle h, cudaStream_t st);
 cudaError_t launch_count_nonfinite(const float* a, size_t n, int* count, cudaStream_t st);
 cudaError_t launch_fill(float* a, size_t n, float v, cudaStream_t st);
+// persistent substep kernel (k_persist.cu): up to Global::budget substeps
+// (armed by launch_loop_arm) of every member in one cooperative launch;
+// Global::iters counts them, bar_err marks a barrier wait that ran out
+// (stall_test: one CTA more is expected than launched, so every wait runs
+// out after 20 ms)
+bool persist_supported(const Params& prm);
+cudaError_t launch_persist(const Params& prm, const Ptrs& P, int stall_test, cudaStream_t st);
 
 }  // namespace umwm

@@ -66,6 +66,7 @@ struct State {
   DevBuf sX, sT;
   long cap = 0, count = 0;
   long holdout = 0;  // trailing stored pairs kept out of training
+  bool loss_weighted = false;  // option "surrogate_loss_weight": energy-weighted loss
   int per_substep = 0;
   bool capture_on = false;
   DevBuf c_pts, c_shift, c_ecopy;
@@ -193,7 +194,8 @@ int backward(int B, float* dloss, cudaStream_t st) {
   if ((rc = forward(S.bX.as<bf16>(), B, S.H1.as<bf16>(), S.H2.as<bf16>(), S.Z1.as<bf16>(), S.Z2.as<bf16>(),
                     S.Yf.as<float>(), nullptr, st)))
     return rc;
-  SCU(launch_loss(S.Yf.as<float>(), S.bT.as<bf16>(), B, S.F0, S.dY.as<bf16>(), dloss, st));
+  SCU(launch_loss(S.Yf.as<float>(), S.bT.as<bf16>(), S.loss_weighted ? S.bX.as<bf16>() : nullptr, B, S.F0,
+                  S.dY.as<bf16>(), dloss, st));
   // layer 3
   SCU(launch_transpose(S.dY.as<bf16>(), B, FPAD, S.dYt.as<bf16>(), st));
   SCU(launch_transpose(S.H2.as<bf16>(), B, HID, S.H2t.as<bf16>(), st));
@@ -345,6 +347,10 @@ int set_option(const std::string& name, double value) {
     S.timing = value != 0;
     S.ms_features = S.ms_gemm = S.ms_apply = 0;
     S.timed_steps = 0;
+    return UMWM_OK;
+  }
+  if (name == "surrogate_loss_weight") {  // 1: energy-weighted training loss (energy_weight)
+    S.loss_weighted = value != 0;
     return UMWM_OK;
   }
   if (name == "surrogate_holdout") {
@@ -537,7 +543,8 @@ int umwm_gpu_surrogate_eval(long first, long count, double* loss) {
     if ((rc = forward(S.bX.as<bf16>(), n, S.H1.as<bf16>(), S.H2.as<bf16>(), S.Z1.as<bf16>(), S.Z2.as<bf16>(),
                       S.Yf.as<float>(), nullptr, S.st)))
       return rc;
-    SCU(launch_loss(S.Yf.as<float>(), S.bT.as<bf16>(), n, S.F0, S.dY.as<bf16>(), dl.as<float>() + b, S.st));
+    SCU(launch_loss(S.Yf.as<float>(), S.bT.as<bf16>(), S.loss_weighted ? S.bX.as<bf16>() : nullptr, n, S.F0,
+                    S.dY.as<bf16>(), dl.as<float>() + b, S.st));
     SCU(cudaStreamSynchronize(S.st));  // h is reused
   }
   std::vector<float> l(nb);

@@ -42,6 +42,14 @@ constexpr int HID = 512;     // hidden width
 constexpr float EPS = 1e-15f;
 constexpr float LN_C0 = -15.f, LN_C1 = 8.f;
 constexpr float TS = 2.f;    // tendency scale
+// Energy weight of a target bin in the weighted loss, from its input feature
+// x = (ln(e + EPS) - LN_C0) / LN_C1: a ramp in ln e from WL0 (e = 1e-9,
+// weight WMIN) to WL1 (e = 1e-5, weight 1)
+constexpr float WL0 = -20.7232658f, WL1 = -11.5129255f, WMIN = 0.01f;
+__host__ __device__ inline float energy_weight(float x) {
+  const float w = (x * LN_C1 + LN_C0 - WL0) / (WL1 - WL0);
+  return w < WMIN ? WMIN : (w > 1.f ? 1.f : w);
+}
 
 // Device kernels (k_sur.cu) ---------------------------------------------------
 
@@ -66,9 +74,12 @@ cudaError_t launch_apply(const Params& prm, const Ptrs& P, const __nv_bfloat16* 
 cudaError_t launch_gather_rows(const __nv_bfloat16* src, const int* idx, int n, int width, __nv_bfloat16* dst,
                                cudaStream_t st);
 cudaError_t launch_transpose(const __nv_bfloat16* src, int rows, int cols, __nv_bfloat16* dst, cudaStream_t st);
-// dY = 2 (Y - T) / (n * F0) over the first F0 columns (0 beyond); loss += sum (Y-T)^2 / (n*F0)
-cudaError_t launch_loss(const float* Y, const __nv_bfloat16* T, int n, int f0, __nv_bfloat16* dY, float* loss,
-                        cudaStream_t st);
+// dY = 2 w (Y - T) / (n * F0) over the first F0 columns (0 beyond);
+// loss += sum w (Y-T)^2 / (n*F0).  w = 1, or with X (the batch's input rows)
+// the energy weight of the bin, energy_weight(X): targets of nearly empty
+// bins (whose log-tendency is noise at the EPS floor) count little
+cudaError_t launch_loss(const float* Y, const __nv_bfloat16* T, const __nv_bfloat16* X, int n, int f0,
+                        __nv_bfloat16* dY, float* loss, cudaStream_t st);
 cudaError_t launch_colsum(const __nv_bfloat16* A, int rows, int cols, float* out, cudaStream_t st);
 cudaError_t launch_adam(float* w, const float* g, float* m, float* v, long n, float lr, float b1, float b2,
                         float eps, float c1, float c2, cudaStream_t st);

@@ -15,6 +15,7 @@
 #include <functional>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <limits>
@@ -99,7 +100,9 @@ struct MemberHost {
 // tuner is active the inner loop runs host-driven and substep s launches each
 // kernel with its candidate s mod n (round-robin, `reps` times each), timed
 // with CUDA events on the model's stream; once a kernel has all its samples
-// it keeps the candidate with the smallest mean time.  The tuner measures the
+// it keeps the candidate with the smallest median time (timing noise only
+// adds time, and the interleaving spreads drift over all candidates).  The
+// tuner measures the
 // model's real substeps, so tuning costs no extra work.  Register budgets and
 // prefetch distances do not change any result (mode 1); the direction mapping
 // changes the summation order of the partial sums (mode 2, results differ by
@@ -110,8 +113,7 @@ struct TuneCand {
 };
 struct KernelTune {
   std::vector<TuneCand> cands;
-  std::vector<double> ms;
-  std::vector<int> n;
+  std::vector<std::vector<float>> ms;  // samples per candidate
   int best = -1;
 };
 enum { TK_PHYS = 0, TK_INTEG, TK_ADVECT, TK_N };
@@ -119,7 +121,7 @@ struct Tuner {
   int mode = 0;         // 0 off, 1 register budgets and prefetch, 2 also the direction mapping
   bool active = false;  // measuring
   bool done = false;    // a choice is in place (tuned or from the cache)
-  int reps = 2;
+  int reps = 5;  // samples per candidate; the median decides (timing noise only adds time)
   int step = 0;         // substeps measured so far
   KernelTune k[TK_N];
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> kev;  // pending (kernel, events)
@@ -178,6 +180,14 @@ struct Model {
   long long kcnt[K_NK] = {0};
   float *E = nullptr, *ES = nullptr, *TAB = nullptr;
   Tuner tune;
+  // persistent substep kernel (option "persistent"): its launch captured in a
+  // graph once per launch configuration (pgraph_state 1), or launched
+  // directly where the capture is refused (-1); 0: not tried yet
+  bool persistent = false;
+  int stall_test = 0;  // option "persistent_stall_test": the next launch's barrier waits run out
+  cudaGraph_t pgraph = nullptr;
+  cudaGraphExec_t pgraph_exec = nullptr;
+  int pgraph_state = 0;
 
   ~Model() {
     for (cudaEvent_t e : evpool) cudaEventDestroy(e);
@@ -187,6 +197,8 @@ struct Model {
     if (flag_h) cudaFreeHost(flag_h);
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (graph) cudaGraphDestroy(graph);
+    if (pgraph_exec) cudaGraphExecDestroy(pgraph_exec);
+    if (pgraph) cudaGraphDestroy(pgraph);
   }
 };
 
@@ -236,6 +248,42 @@ void collect_timings(Model& M) {
 void drop_graph(Model& M) {  // the captured inner loop holds the old launch configuration
   if (M.graph_exec) { cudaGraphExecDestroy(M.graph_exec); M.graph_exec = nullptr; }
   if (M.graph) { cudaGraphDestroy(M.graph); M.graph = nullptr; }
+  if (M.pgraph_exec) { cudaGraphExecDestroy(M.pgraph_exec); M.pgraph_exec = nullptr; }
+  if (M.pgraph) { cudaGraphDestroy(M.pgraph); M.pgraph = nullptr; }
+  if (M.pgraph_state == 1) M.pgraph_state = 0;
+}
+
+// One launch of the persistent substep kernel (budget armed before): the
+// graph holding it, captured on first use, or a direct cooperative launch
+// when the capture is refused or the stall test is armed.
+int persist_launch(Model& M) {
+  if (M.stall_test) {
+    M.stall_test = 0;
+    CU(launch_persist(M.prm, M.P, 1, M.st));
+    return UMWM_OK;
+  }
+  if (M.pgraph_state == 0) {
+    cudaError_t e = cudaStreamBeginCapture(M.st, cudaStreamCaptureModeThreadLocal);
+    cudaError_t el = e == cudaSuccess ? launch_persist(M.prm, M.P, 0, M.st) : e;
+    cudaGraph_t g = nullptr;
+    cudaError_t ec = e == cudaSuccess ? cudaStreamEndCapture(M.st, &g) : e;
+    cudaError_t ei = (el == cudaSuccess && ec == cudaSuccess) ? cudaGraphInstantiate(&M.pgraph_exec, g, 0) : el;
+    if (el == cudaSuccess && ec == cudaSuccess && ei == cudaSuccess) {
+      M.pgraph = g;
+      M.pgraph_state = 1;
+    } else {
+      if (g) cudaGraphDestroy(g);
+      M.pgraph_exec = nullptr;
+      cudaGetLastError();  // the refused capture is not an error of the run
+      M.pgraph_state = -1;
+    }
+  }
+  if (M.pgraph_state == 1) {
+    CU(cudaGraphLaunch(M.pgraph_exec, M.st));
+  } else {
+    CU(launch_persist(M.prm, M.P, 0, M.st));
+  }
+  return UMWM_OK;
 }
 
 std::string tune_key(const Model& M) {
@@ -295,8 +343,7 @@ void tune_start(Model& M, int mode) {
       for (int mb : minbs)
         for (int pf : pfs) K.cands.push_back({g4, mb, pf});
     }
-    K.ms.assign(K.cands.size(), 0.0);
-    K.n.assign(K.cands.size(), 0);
+    K.ms.assign(K.cands.size(), {});
     K.best = -1;
   }
   T.active = true;
@@ -332,8 +379,7 @@ void tune_collect(Model& M) {
     KernelTune& K = T.k[kv.first];
     if (K.best >= 0) continue;
     const int c = (int)(T.step % K.cands.size());
-    K.ms[c] += ms;
-    K.n[c] += 1;
+    K.ms[c].push_back(ms);
   }
   T.kev.clear();
   T.used = 0;
@@ -344,8 +390,12 @@ void tune_collect(Model& M) {
     if (K.best >= 0) continue;
     if (T.step < (int)K.cands.size() * T.reps) { all = false; continue; }
     double bm = 1e300;
-    for (size_t c = 0; c < K.cands.size(); ++c)
-      if (K.n[c] > 0 && K.ms[c] / K.n[c] < bm) { bm = K.ms[c] / K.n[c]; K.best = (int)c; }
+    for (size_t c = 0; c < K.cands.size(); ++c) {
+      std::vector<float> v = K.ms[c];
+      if (v.empty()) continue;
+      std::nth_element(v.begin(), v.begin() + v.size() / 2, v.end());
+      if (v[v.size() / 2] < bm) { bm = v[v.size() / 2]; K.best = (int)c; }
+    }
     if (K.best < 0) K.best = 0;
   }
   if (!all) return;
@@ -1464,6 +1514,23 @@ int run_impl(Model& M, const std::string& start, const std::string& stop) {
     for (long long inner = 0;;) {
       if (inner > 10000000LL) return fail(UMWM_ERR_TIMEOUT, "umwm_run: more than 1e7 substeps in one dtg (dts stuck at 0?)");
       if (M.max_substeps >= 0 && M.substeps >= M.max_substeps) return finish_run(M);
+      if (M.persistent && !M.first && !M.ktime && !M.tune.active && !sur::active() && !sur::capturing() &&
+          persist_supported(M.prm)) {
+        long long budget = GRAPH_CHUNK;
+        if (M.max_substeps >= 0) budget = std::min(budget, M.max_substeps - M.substeps);
+        CU(launch_loop_arm(M.d_glob, (int)budget, M.st));
+        if ((rc = persist_launch(M))) return rc;
+        CU(cudaMemcpyAsync(M.flag_h, M.d_glob, sizeof(Global), cudaMemcpyDeviceToHost, M.st));
+        CU(cudaStreamSynchronize(M.st));
+        if (M.flag_h->bar_err)
+          return fail(UMWM_ERR_TIMEOUT, "umwm_run: a grid barrier wait of the persistent substep kernel ran out");
+        const int it = M.flag_h->iters;
+        M.substeps += it;
+        M.launches += 3;
+        inner += it;
+        if (M.flag_h->not_done == 0) break;
+        continue;
+      }
       if (M.use_graph && !M.first && !M.ktime && !M.tune.active && !sur::active() && !sur::capturing()) {
         if ((rc = build_graph(M))) return rc;
         long long budget = GRAPH_CHUNK;
@@ -2103,6 +2170,13 @@ int umwm_gpu_set_option(const char* name, double value) {
     return UMWM_OK;
   }
   if (s == "use_graph") { M->use_graph = value != 0; return UMWM_OK; }
+  if (s == "persistent") {
+    if (value != 0 && !persist_supported(M->prm))
+      return fail(UMWM_ERR_UNSUPPORTED, "persistent needs pm = 36 and one direction mapping for all three kernels");
+    M->persistent = value != 0;
+    return UMWM_OK;
+  }
+  if (s == "persistent_stall_test") { M->stall_test = value != 0 ? 1 : 0; return UMWM_OK; }
   if (s == "stress_ocn") {
     M->ocn_every = value != 0;
     return M->ocn_every ? ensure_ocn(*M) : UMWM_OK;
@@ -2159,10 +2233,34 @@ double umwm_gpu_get_stat(const char* name) {
   if (s == "gpu_ms") return M->last_gpu_ms;
   if (s == "bin_updates") return M->last_bins;
   if (s == "launches") return (double)M->launches;
+  if (s == "persistent_graph") return (double)M->pgraph_state;  // 1 captured, -1 direct launches, 0 not run
   if (s == "cut_count") {  // bins the non-negativity cut changed since count_cut was set
     unsigned long long c = 0;
     if (cudaMemcpy(&c, &M->d_glob->cut_count, sizeof c, cudaMemcpyDeviceToHost) != cudaSuccess) return -1.0;
     return (double)c;
+  }
+  // the tuner's measurements: "tune_n:<kernel>" candidates, "tune_cfg:<kernel>:<i>"
+  // candidate i's configuration (encoded as config:*), "tune_ms:<kernel>:<i>"
+  // its median time in ms (-1 before it was measured)
+  if (s.compare(0, 5, "tune_") == 0) {
+    const size_t c1 = s.find(':');
+    if (c1 == std::string::npos) return -1.0;
+    const size_t c2 = s.find(':', c1 + 1);
+    const std::string what = s.substr(0, c1), kn = s.substr(c1 + 1, c2 == std::string::npos ? std::string::npos : c2 - c1 - 1);
+    const int k = kn == "phys" ? TK_PHYS : kn == "integ" ? TK_INTEG : kn == "advect" ? TK_ADVECT : -1;
+    if (k < 0) return -1.0;
+    const KernelTune& K = M->tune.k[k];
+    if (what == "tune_n") return (double)K.cands.size();
+    const int i = c2 == std::string::npos ? -1 : std::atoi(s.c_str() + c2 + 1);
+    if (i < 0 || i >= (int)K.cands.size()) return -1.0;
+    if (what == "tune_cfg") return (K.cands[i].g4 ? 4 : 2) * 100.0 + K.cands[i].minb * 10.0 + K.cands[i].pf;
+    if (what == "tune_ms") {
+      std::vector<float> v = K.ms[i];
+      if (v.empty()) return -1.0;
+      std::nth_element(v.begin(), v.begin() + v.size() / 2, v.end());
+      return v[v.size() / 2];
+    }
+    return -1.0;
   }
   if (s == "autotune_active") return M->tune.active ? 1.0 : 0.0;
   if (s == "autotune_done") return M->tune.done ? 1.0 : 0.0;
