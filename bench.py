@@ -391,21 +391,30 @@ def _angle_err_deg(a, b):
     return np.degrees(np.abs(d))
 
 
+def _parse_budgets(text):
+    """'tol:tol_level,...' -> [(tol, tol_level), ...]"""
+    out = []
+    for part in text.split(","):
+        a, b = part.split(":")
+        out.append((float(a), float(b)))
+    return out
+
+
 def run_surrogate(args):
     """Learned source-term surrogate (hurricane forcing on the size x size
     grid).  Pairs come from plain GPU runs of a random-field domain and a
-    hurricane domain with other seeds; the network trains on the GPU; then
-    the same hurricane case runs args.hours with the plain path and with the
-    surrogate (energy-budget fallback on), and the surrogate's Hs, Tp (peak
-    period, dwp) and mean direction are compared with the plain run."""
+    hurricane domain with other seeds; the network trains on the GPU (three
+    phases of decreasing learning rate, energy-weighted loss, 2 % of the
+    pairs held out); then, for each energy budget of --sur-budgets, the same
+    hurricane case runs args.hours with the surrogate (fallback on), and its
+    Hs, Tp (peak period, dwp) and mean direction are compared with the plain
+    run, and on a --sur-fp64-size grid with the fp64 oracle."""
     rank, world, local_rank = rank_info()
     import umwm_gb300 as U
     from umwm_gb300 import configs
 
     U.set_option("device", local_rank)
     U.surrogate_init(37, 36, seed=7)
-    U.set_option("surrogate_tol", args.sur_tol)
-    U.set_option("surrogate_tol_level", args.sur_tol_level)
     U.surrogate_capture(args.pairs, args.pts_per_substep)
     gen = []
     t0 = time.perf_counter()
@@ -442,10 +451,12 @@ def run_surrogate(args):
 
     ev = configs.hurricane(mm=args.size, nm=args.size, hours=args.hours, seed=5)
 
-    def run(sur):
+    def run(case, sur, substep_cap=None):
+        """One run of a case; the surrogate run stops at the first non-finite
+        Hs/ustar or past substep_cap substeps.  Hs is kept every hour."""
         U.clear_inputs()
-        ev.stage(U)
-        U.umwm_initialize(nml_text=ev.nml)
+        case.stage(U)
+        U.umwm_initialize(nml_text=case.nml)
         U.set_option("use_graph", 0 if sur else 1)
         U.set_option("surrogate", 1 if sur else 0)
         U.set_option("surrogate_timing", 1 if sur else 0)
@@ -454,26 +465,26 @@ def run_surrogate(args):
         hourly = []
         stopped = None
         if sur:
-            # a diverging run stops at the first non-finite Hs/ustar, or when it
-            # needs more than three times the plain run's substeps
             U.set_option("check_finite", 1)
-            U.set_option("max_substeps", 3 * plain_substeps)
+            if substep_cap:
+                U.set_option("max_substeps", substep_cap)
         for h in range(int(args.hours)):  # hour by hour: Hs after every hour
             try:
-                U.umwm_run(configs._time_str(ev.start, 3600 * h), configs._time_str(ev.start, 3600 * (h + 1)))
+                U.umwm_run(configs._time_str(case.start, 3600 * h), configs._time_str(case.start, 3600 * (h + 1)))
             except U.UmwmError as exc:
                 stopped = {"hour": h, "reason": str(exc)}
                 break
             gpu_ms += U.stat("gpu_ms")
             bins += U.stat("bin_updates")
             hourly.append(U.get_field("ht").astype(np.float64))
-            if sur and U.dims()["substeps"] >= 3 * plain_substeps:
+            if sur and substep_cap and U.dims()["substeps"] >= substep_cap:
                 stopped = {"hour": h + 1, "reason": "more than 3x the plain run's substeps"}
                 break
         U.set_option("check_finite", 0)
         U.set_option("max_substeps", -1)
         out = {"gpu_ms": gpu_ms, "bins": bins, "substeps": U.dims()["substeps"], "hourly": hourly, "stopped": stopped,
-               "ht": U.get_field("ht"), "dwp": U.get_field("dwp"), "mwd": U.get_field("mwd"),
+               "ht": U.get_field("ht").astype(np.float64), "dwp": U.get_field("dwp").astype(np.float64),
+               "mwd": U.get_field("mwd").astype(np.float64),
                "points": U.stat("surrogate_points") - p0, "fallback": U.stat("surrogate_fallback") - f0}
         if sur:
             out.update({k: U.stat("surrogate_" + k) for k in ("ms_features", "ms_gemm", "ms_apply", "timed_steps",
@@ -483,110 +494,86 @@ def run_surrogate(args):
         U.umwm_finalize()
         return out
 
-    plain_substeps = 10 ** 9
-    plain = run(False)
-    plain_substeps = plain["substeps"]
-    sur = run(True)
-    nh = len(sur["hourly"])
-    ended = sur["stopped"] is None
-    # errors at the last hour the surrogate run completed
-    hp = plain["hourly"][nh - 1] if nh else plain["ht"].astype(np.float64)
-    hs = sur["hourly"][nh - 1] if nh else np.full_like(hp, np.nan)
-    hourly_err = []
-    for a, b in zip(sur["hourly"], plain["hourly"]):
-        m = b > 1e-3
-        fin = np.isfinite(a) & m
-        hourly_err.append({"mean_abs_rel": float(np.abs(a - b)[fin].mean() / b[fin].mean()) if fin.any() else None,
-                           "nonfinite_frac": float(1.0 - fin.sum() / max(m.sum(), 1))})
-    wet = (hp > 1e-3) & np.isfinite(hs)
-    hs_err = None
-    if wet.any():
-        hs_err = {"at_hour": nh, "mean_abs_rel": float(np.abs(hs - hp)[wet].mean() / hp[wet].mean()),
-                  "rel_l2": float(np.linalg.norm((hs - hp)[wet]) / np.linalg.norm(hp[wet])),
-                  "p99_rel": float(np.percentile(np.abs(hs - hp)[wet] / hp[wet], 99)),
-                  "domain_mean_rel": float(abs(hs[wet].mean() - hp[wet].mean()) / hp[wet].mean())}
-    tp_err = dir_err = None
-    if ended and wet.any():  # peak period and direction at the end of the run
-        tp_err = {"mean_abs_rel": float((np.abs(sur["dwp"] - plain["dwp"])[wet] / plain["dwp"][wet]).mean()),
-                  "same_bin_frac": float((sur["dwp"] == plain["dwp"])[wet].mean())}
-        dir_err = {"mean_abs_deg": float(_angle_err_deg(sur["mwd"], plain["mwd"])[wet].mean()),
-                   "hs_weighted_deg": float((_angle_err_deg(sur["mwd"], plain["mwd"]) * hp)[wet].sum()
-                                            / hp[wet].sum())}
-    # against the fp64 oracle: the same hurricane on a smaller grid, run with
-    # the plain path, the surrogate and the fp64 oracle
-    sur_fp64 = None
+    def errors(a, b, label):
+        """Hs, Tp and mean-direction errors of run a against the fields b at
+        the end of a completed run"""
+        if a.get("stopped") is not None:
+            return None
+        wet = (b["ht"] > 1e-3) & np.isfinite(a["ht"])
+        if not wet.any():
+            return None
+        rel = np.abs(a["ht"] - b["ht"])[wet] / b["ht"][wet]
+        return {"against": label, "hs_mean_rel": float(rel.mean()), "hs_max_rel": float(rel.max()),
+                "hs_p99_rel": float(np.percentile(rel, 99)),
+                "hs_rel_l2": float(np.linalg.norm((a["ht"] - b["ht"])[wet]) / np.linalg.norm(b["ht"][wet])),
+                "tp_mean_rel": float((np.abs(a["dwp"] - b["dwp"])[wet] / b["dwp"][wet]).mean()),
+                "tp_same_bin_frac": float((np.abs(a["dwp"] - b["dwp"]) <= 1e-5 * b["dwp"])[wet].mean()),
+                "dir_mean_abs_deg": float(_angle_err_deg(a["mwd"], b["mwd"])[wet].mean()),
+                "dir_hs_weighted_deg": float((_angle_err_deg(a["mwd"], b["mwd"]) * b["ht"])[wet].sum()
+                                             / b["ht"][wet].sum())}
+
+    plain = run(ev, False)
+    v_plain = plain["bins"] / (plain["gpu_ms"] / 1e3)
+    # the fp64 oracle on the smaller grid, and the plain GPU run there
+    small = ref64 = plain_small = None
     if args.sur_fp64_size > 0:
         from oracle import pyoracle
 
         small = configs.hurricane(mm=args.sur_fp64_size, nm=args.sur_fp64_size, hours=args.hours, seed=5)
-        fields = {}
-        for tag, use in (("plain", False), ("surrogate", True)):
-            U.clear_inputs()
-            small.stage(U)
-            U.umwm_initialize(nml_text=small.nml)
-            U.set_option("surrogate", 1 if use else 0)
-            p0, f0 = U.stat("surrogate_points"), U.stat("surrogate_fallback")
-            U.set_option("check_finite", 1)
-            try:
-                U.umwm_run(small.start, small.stop)
-                fields[tag] = {k: U.get_field(k).astype(np.float64) for k in ("ht", "dwp", "mwd")}
-                fields[tag]["fallback"] = (U.stat("surrogate_fallback") - f0) / max(U.stat("surrogate_points") - p0, 1)
-            except U.UmwmError as exc:
-                fields[tag] = {"error": str(exc)}
-            U.set_option("surrogate", 0)
-            U.umwm_finalize()
+        plain_small = run(small, False)
         pyoracle.set_threads(os.cpu_count() or 1)
         o = pyoracle.Oracle(small.nml, 64)
         small.stage(o)
         o.initialize()
         o.run(small.start, small.stop)
-        ref = {k: np.asarray(o.get(k), dtype=np.float64) for k in ("ht", "dwp", "mwd")}
-        wet = ref["ht"] > 1e-3
-        sur_fp64 = {"case": "hurricane %dx%d dx=2km seed 5, %g h" % (args.sur_fp64_size, args.sur_fp64_size,
-                                                                      args.hours)}
-        for tag, f in fields.items():
-            if "error" in f:
-                sur_fp64[tag] = f
-                continue
-            rel = np.abs(f["ht"] - ref["ht"])[wet] / ref["ht"][wet]
-            sur_fp64[tag] = {"hs_max_rel": float(rel.max()), "hs_mean_rel": float(rel.mean()),
-                             "hs_p99_rel": float(np.percentile(rel, 99)),
-                             "tp_mean_rel": float((np.abs(f["dwp"] - ref["dwp"])[wet] / ref["dwp"][wet]).mean()),
-                             "tp_same_bin_frac": float((np.abs(f["dwp"] - ref["dwp"]) <= 1e-5 * ref["dwp"])[wet].mean()),
-                             "dir_mean_abs_deg": float(_angle_err_deg(f["mwd"], ref["mwd"])[wet].mean()),
-                             "fallback_fraction": float(f["fallback"])}
+        ref64 = {k: np.asarray(o.get(k), dtype=np.float64) for k in ("ht", "dwp", "mwd")}
         del o
-    v_sur = sur["bins"] / (sur["gpu_ms"] / 1e3) if sur["gpu_ms"] > 0 else 0.0
-    v_plain = plain["bins"] / (plain["gpu_ms"] / 1e3)
     flops_row = 2.0 * (1344 * 512 + 512 * 512 + 512 * 1344)
-    gemm_tflops = (flops_row * sur["rows"] * sur["timed_steps"] / (sur["ms_gemm"] / 1e3) / 1e12
-                   if sur["ms_gemm"] > 0 else None)
+    budgets = []
+    for tol, tol_level in _parse_budgets(args.sur_budgets):
+        U.set_option("surrogate_tol", tol)
+        U.set_option("surrogate_tol_level", tol_level)
+        sur = run(ev, True, substep_cap=3 * plain["substeps"])
+        v_sur = sur["bins"] / (sur["gpu_ms"] / 1e3) if sur["gpu_ms"] > 0 and sur["stopped"] is None else 0.0
+        ts = max(sur["timed_steps"], 1)
+        b = {"tol": tol, "tol_level": tol_level, "value": v_sur, "surrogate_over_plain": v_sur / v_plain,
+             "substeps": sur["substeps"], "stopped": sur["stopped"],
+             "fallback_fraction": sur["fallback"] / max(sur["points"], 1),
+             "vs_plain": errors(sur, plain, "plain GPU run, %dx%d" % (args.size, args.size)),
+             "hs_vs_plain_hourly_mean_rel": [float(np.abs(x - y)[y > 1e-3].mean() / y[y > 1e-3].mean())
+                                             for x, y in zip(sur["hourly"], plain["hourly"])],
+             "ms_per_step": {"features": sur["ms_features"] / ts, "gemm": sur["ms_gemm"] / ts,
+                             "apply": sur["ms_apply"] / ts},
+             "gemm_tflops": (flops_row * sur["rows"] * sur["timed_steps"] / (sur["ms_gemm"] / 1e3) / 1e12
+                             if sur["ms_gemm"] > 0 else None)}
+        if small is not None:
+            ss = run(small, True, substep_cap=3 * plain_small["substeps"])
+            b["vs_fp64"] = errors(ss, ref64, "fp64 oracle, %dx%d" % (args.sur_fp64_size, args.sur_fp64_size))
+            b["vs_fp64_fallback_fraction"] = ss["fallback"] / max(ss["points"], 1)
+            b["vs_fp64_stopped"] = ss["stopped"]
+        budgets.append(b)
+        print(json.dumps({"budget": b}), file=sys.stderr, flush=True)
+    first = budgets[0]
     pk, pk_sus, pk_kind = peak_bf16()
-    line = {"metric": METRIC, "value": v_sur, "unit": UNIT, "n_gpus": 1, "steps": sur["substeps"], "warmup": 0,
-            "ms_per_step": sur["gpu_ms"] / max(sur["substeps"], 1), "higher_is_better": True, "scaling": "weak",
+    gt = first["gemm_tflops"]
+    line = {"metric": METRIC, "value": first["value"], "unit": UNIT, "n_gpus": 1, "steps": first["substeps"],
+            "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16 (MLP) / f32 (spectrum)", "data": "synthetic",
             "config": {"workload": "surrogate: hurricane %dx%d dx=2km seed 5, %g h, JONSWAP Hs 0.2 m start; MLP "
-                                   "1344-512-512-1344 GELU bf16/f32-acc; energy-budget tolerances %g (total), %g "
-                                   "(level, wind-weighted)" % (args.size, args.size, args.hours, args.sur_tol,
-                                                               args.sur_tol_level),
-                       "pairs": int(U.stat("surrogate_pairs")), "pair_sources": gen,
-                       "train_steps": int(len(losses)), "batch": 8192},
+                                   "1344-512-512-1344 GELU bf16/f32-acc; energy budgets %s (total:level)"
+                                   % (args.size, args.size, args.hours, args.sur_budgets),
+                       "pairs": npairs, "pair_sources": gen, "train_steps": int(len(losses)), "batch": 8192},
             "plain": {"value": v_plain, "gpu_ms": plain["gpu_ms"], "substeps": plain["substeps"]},
-            "surrogate_over_plain": v_sur / v_plain,
-            "fallback_fraction": sur["fallback"] / max(sur["points"], 1),
-            "hs_error_vs_plain": hs_err, "tp_error_vs_plain": tp_err, "dir_error_vs_plain": dir_err,
-            "hs_error_vs_plain_hourly": hourly_err, "surrogate_run_stopped": sur["stopped"],
-            "nonfinite_points_end": int((~np.isfinite(hs)).sum()),
+            "plain_vs_fp64": errors(plain_small, ref64, "fp64 oracle, %dx%d" % (args.sur_fp64_size,
+                                                                                args.sur_fp64_size))
+            if small is not None else None,
+            "budgets": budgets,
             "train": {"seconds": t_train, "steps": int(len(losses)), "weighted_loss": bool(args.sur_weighted),
                       "loss_first": float(losses[:20].mean()), "loss_last": float(losses[-20:].mean()),
                       "heldout_pairs": nhold, "heldout_loss": held},
-            "vs_fp64": sur_fp64,
             "generate_seconds": t_gen,
-            "surrogate_ms_per_step": {"features": sur["ms_features"] / max(sur["timed_steps"], 1),
-                                      "gemm": sur["ms_gemm"] / max(sur["timed_steps"], 1),
-                                      "apply": sur["ms_apply"] / max(sur["timed_steps"], 1)},
-            "roofline": {"bound": "tensor", "kernel": "k_gemm (3 layers)", "achieved": gemm_tflops, "peak": pk_sus,
-                         "unit": "TFLOP/s", "frac": (gemm_tflops / pk_sus) if gemm_tflops else None,
+            "roofline": {"bound": "tensor", "kernel": "k_gemm (3 layers)", "achieved": gt, "peak": pk_sus,
+                         "unit": "TFLOP/s", "frac": (gt / pk_sus) if gt else None,
                          "peak_kind": pk_kind + " sustained", "traffic": None}}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -746,8 +733,8 @@ def main():
     ap.add_argument("--sur-fp64-size", type=int, default=120,
                     help="grid of the surrogate's comparison with the fp64 oracle (0: none)")
     ap.add_argument("--hours", type=float, default=12.0)
-    ap.add_argument("--sur-tol", type=float, default=0.02, help="surrogate total-energy budget per substep")
-    ap.add_argument("--sur-tol-level", type=float, default=0.1, help="surrogate per-level energy budget")
+    ap.add_argument("--sur-budgets", default="0.02:0.1,0.005:0.03,0.002:0.01",
+                    help="surrogate energy budgets to evaluate, total:level per substep, comma separated")
     ap.add_argument("--members", type=int, default=64)
     ap.add_argument("--persistent", action="store_true",
                     help="ensemble arms run the inner loop as the persistent substep kernel")

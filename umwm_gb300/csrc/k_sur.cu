@@ -14,7 +14,7 @@ namespace sur {
 namespace {
 
 constexpr int PITCHW = FPAD / 2 + 1;  // 32-bit words per staged row (odd: conflict-free columns)
-constexpr int UNR = 6;                 // spectrum loads in flight per warp in the bin loops
+constexpr int UNR = 12;                // spectrum loads in flight per warp in the bin loops
 constexpr int TILE_SMEM = 32 * PITCHW * 4;
 
 struct PointInfo {
@@ -38,20 +38,11 @@ __device__ __forceinline__ PointInfo point_info(const Params& prm, const Ptrs& P
 
 __device__ __forceinline__ float feature(float e) { return (logf(fmaxf(e, 0.f) + EPS) - LN_C0) * (1.f / LN_C1); }
 
-// Surrogate step of one bin: the predicted log-tendency, capped above by the
-// growth the wind input allows over dts (dts * max(Sin, 0) + GROWTH_SLACK).
-// Without wind input a bin cannot grow in the plain step, so the cap stops a
-// network error from feeding energy into bins the forcing does not reach.
+// Growth allowance of the surrogate step (k_apply): a bin's predicted
+// log-tendency is capped by dts * max(Sin, 0) + GROWTH_SLACK.  Without wind
+// input a bin cannot grow in the plain step, so the cap stops a network
+// error from feeding energy into bins the forcing does not reach.
 constexpr float GROWTH_SLACK = 0.02f;
-__device__ __forceinline__ float step_bin(const Params& prm, const Ptrs& P, const WindIn& wi, float dts, float wdir,
-                                          float e, float y, int o, int p, int j, float& sin_pos) {
-  const float* T = P.TAB + tidx(prm, o, 0, j);
-  const float sin_ = sin_bin(prm, wi, cosf(wdir - prm.th[p]), prm.cth[p], prm.sth[p], T[T_LOGL2Z * 32],
-                             T[T_CP0 * 32], T[T_FKOVG * 32], o >= wi.oc);
-  sin_pos = fmaxf(sin_, 0.f);
-  const float d = fminf(TS * y, dts * sin_pos + GROWTH_SLACK);
-  return fmaxf((fmaxf(e, 0.f) + EPS) * expf(d) - EPS, 0.f);
-}
 
 __device__ __forceinline__ __nv_bfloat16* row_h(uint32_t* tile, int r) {
   return reinterpret_cast<__nv_bfloat16*>(tile + r * PITCHW);
@@ -147,22 +138,30 @@ __global__ void k_targets(const Params prm, const Ptrs P, const int* pts, int n,
   }
 }
 
+// Apply step of one 32-point block (lane = point).  Each warp takes every
+// eighth frequency level: it stages the level's row segment of each point's
+// network output in shared memory (the rotation by the point's wind bin is
+// then a shared-memory index), reads the level's table values once, and
+// sums the level's energy before and after in registers, so no level sum
+// needs an atomic.  Pass 1 forms ef for every bin and writes E* = (e + ef)/2
+// and the monitor's sums; the points that pass get ef at the levels above
+// the cut-off in pass 2 (E* of the failing points is rewritten by the
+// fallback integration).
 __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, const __nv_bfloat16* Y, float tol,
                                                float tol_level, unsigned char* fb_pt, int* fb_tile,
                                                unsigned long long* counts) {
-  extern __shared__ uint32_t tile[];
+  extern __shared__ uint32_t dyn[];
   __shared__ float red0[8][32], red1[8][32], red2[8][32], red3[8][32];
   __shared__ float lev0[MAX_OM][32], lev1[MAX_OM][32];  // energy of each frequency level before / after
   __shared__ int s_ok[32], s_s[32], s_pass[32];
   __shared__ WindIn s_wi[32];
-  __shared__ float s_wdir[32], s_dts[32];
-  for (int i = threadIdx.x; i < MAX_OM * 32; i += blockDim.x) {
-    (&lev0[0][0])[i] = 0.f;
-    (&lev1[0][0])[i] = 0.f;
-  }
+  __shared__ float s_dts[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int jb = blockIdx.x, j = jb * 32 + lane;
-  const int NP = prm.P, F0 = prm.O * prm.P;
+  const int NP = prm.P, O = prm.O;
+  const int YP = NP | 1;  // staged row pitch (odd: conflict-free columns)
+  float* cwt = reinterpret_cast<float*>(dyn);                                  // [NP][32]
+  uint16_t* yb = reinterpret_cast<uint16_t*>(dyn + NP * 32) + warp * 32 * YP;  // this warp's [32][YP]
   if (warp == 0) {
     const PointInfo q = point_info(prm, P, j);
     s_ok[lane] = q.ok;
@@ -170,47 +169,65 @@ __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, c
     if (q.ok) {
       const Member& M = prm.mem[prm.tile_mem[j / TILE]];
       s_wi[lane] = load_wind(prm, P, j, apt(M, j), P.ustar[j]);
-      s_wdir[lane] = q.psi;
       s_dts[lane] = M.ctl->dts;
     }
+    for (int p = 0; p < NP; ++p) cwt[p * 32 + lane] = q.ok ? cosf(q.psi - prm.th[p]) : 0.f;
   }
-  const uint32_t* Y32 = reinterpret_cast<const uint32_t*>(Y);
-  for (int rr = warp; rr < 32; rr += 8)
-    for (int k = lane; k < FPAD / 2; k += 32) tile[rr * PITCHW + k] = Y32[(size_t)(jb * 32 + rr) * (FPAD / 2) + k];
   __syncthreads();
   const int ok = s_ok[lane], s = s_s[lane];
-  const __nv_bfloat16* h = row_h(tile, lane);
   const WindIn wi = s_wi[lane];
-  const float wdir = s_wdir[lane], dts = s_dts[lane];
+  const float dts = s_dts[lane];
+  const uint16_t* Yr = reinterpret_cast<const uint16_t*>(Y) + (size_t)j * FPAD;  // this point's output row
+  // stage this point's output at level o (NP bf16, 4-byte aligned: NP is even)
+  auto stage = [&](int o) {
+    __syncwarp();
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(Yr + o * NP);
+    for (int k = 0; k < NP / 2; ++k) {
+      const uint32_t v = ok ? src[k] : 0u;
+      yb[lane * YP + 2 * k] = (uint16_t)(v & 0xffffu);
+      yb[lane * YP + 2 * k + 1] = (uint16_t)(v >> 16);
+    }
+    __syncwarp();
+  };
+  // ef of bin (o, p): the predicted log-tendency, capped above by the growth
+  // the wind input allows over dts
+  auto step = [&](int p, float e, float logl2z, float cp0, float fkovg, bool tail, float& sp) {
+    int pr = p - s;
+    if (pr < 0) pr += NP;
+    const float y = __uint_as_float((uint32_t)yb[lane * YP + pr] << 16);
+    sp = fmaxf(sin_bin(prm, wi, cwt[p * 32 + lane], prm.cth[p], prm.sth[p], logl2z, cp0, fkovg, tail), 0.f);
+    const float d = fminf(TS * y, dts * sp + GROWTH_SLACK);
+    return fmaxf((fmaxf(e, 0.f) + EPS) * expf(d) - EPS, 0.f);
+  };
   float m0 = 0.f, m1 = 0.f, w0 = 0.f, w1 = 0.f;  // energy, and energy where the wind feeds (weight Sin)
-  if (ok) {
-    for (int b0 = warp; b0 < F0; b0 += 8 * UNR) {
+  for (int o = warp; o < O; o += 8) {
+    stage(o);
+    const float* T = P.TAB + tidx(prm, o, 0, j);
+    const float kdk = T[T_KDK * 32], logl2z = T[T_LOGL2Z * 32], cp0 = T[T_CP0 * 32], fkovg = T[T_FKOVG * 32];
+    const bool tail = o >= wi.oc;
+    float lv0 = 0.f, lv1 = 0.f;
+    for (int p0 = 0; p0 < NP; p0 += UNR) {
       float ev[UNR];
 #pragma unroll
-      for (int u = 0; u < UNR; ++u) {
-        const int b = b0 + 8 * u;
-        const int o = b / NP, p = b - o * NP;
-        ev[u] = b < F0 ? P.E[sidx(prm, o, p, j)] : 0.f;
-      }
+      for (int u = 0; u < UNR; ++u) ev[u] = (p0 + u < NP) ? P.E[sidx(prm, o, p0 + u, j)] : 0.f;
 #pragma unroll
       for (int u = 0; u < UNR; ++u) {
-        const int b = b0 + 8 * u;
-        if (b >= F0) break;
-        const int o = b / NP, p = b - o * NP;
-        int pr = p - s;
-        if (pr < 0) pr += NP;
+        const int p = p0 + u;
+        if (p >= NP) break;
         const float e = ev[u];
         float sp;
-        const float ef = step_bin(prm, P, wi, dts, wdir, e, __bfloat162float(h[o * NP + pr]), o, p, j, sp);
-        const float kdk = P.TAB[tidx(prm, o, T_KDK, j)];
+        const float ef = step(p, e, logl2z, cp0, fkovg, tail, sp);
         m0 += e * kdk;
         m1 += ef * kdk;
         w0 += fmaxf(e, 0.f) * sp * kdk;
         w1 += ef * sp * kdk;
-        atomicAdd(&lev0[o][lane], fmaxf(e, 0.f));
-        atomicAdd(&lev1[o][lane], ef);
+        lv0 += fmaxf(e, 0.f);
+        lv1 += ef;
+        if (ok) P.ES[sidx(prm, o, p, j)] = 0.5f * (e + ef);
       }
     }
+    lev0[o][lane] = lv0;
+    lev1[o][lane] = lv1;
   }
   red0[warp][lane] = m0;
   red1[warp][lane] = m1;
@@ -234,9 +251,9 @@ __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, c
                 isfinite(wb) && fabsf(logf((wb + 1e-30f) / (wa + 1e-30f))) <= tol_level;
     if (pass) {
       float lmax = 0.f;
-      for (int o = 0; o < prm.O; ++o) lmax = fmaxf(lmax, lev0[o][lane]);
+      for (int o = 0; o < O; ++o) lmax = fmaxf(lmax, lev0[o][lane]);
       const float floor_ = 1e-4f * lmax + 1e-30f;
-      for (int o = 0; o < prm.O; ++o)
+      for (int o = 0; o < O; ++o)
         if (!(fabsf(logf((lev1[o][lane] + floor_) / (lev0[o][lane] + floor_))) <= tol_level)) pass = false;
     }
     s_pass[lane] = pass ? 1 : 0;
@@ -250,27 +267,20 @@ __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, c
     }
   }
   __syncthreads();
-  if (!s_pass[lane]) return;
-  for (int b0 = warp; b0 < F0; b0 += 8 * UNR) {
-    float ev[UNR];
-#pragma unroll
-    for (int u = 0; u < UNR; ++u) {
-      const int b = b0 + 8 * u;
-      const int o = b / NP, p = b - o * NP;
-      ev[u] = b < F0 ? P.E[sidx(prm, o, p, j)] : 0.f;
-    }
-#pragma unroll
-    for (int u = 0; u < UNR; ++u) {
-      const int b = b0 + 8 * u;
-      if (b >= F0) break;
-      const int o = b / NP, p = b - o * NP;
-      int pr = p - s;
-      if (pr < 0) pr += NP;
+  // pass 2: ef above the cut-off of the passing points (as the integration:
+  // E* only at the propagated levels); lanes of failing points idle in it
+  const bool pass = s_pass[lane] != 0;
+  if (!__any_sync(0xffffffffu, pass)) return;
+  for (int o = warp; o < O; o += 8) {
+    if (!__any_sync(0xffffffffu, pass && o >= wi.oc)) continue;
+    stage(o);
+    if (!(pass && o >= wi.oc)) continue;
+    const float* T = P.TAB + tidx(prm, o, 0, j);
+    const float logl2z = T[T_LOGL2Z * 32], cp0 = T[T_CP0 * 32], fkovg = T[T_FKOVG * 32];
+    for (int p = 0; p < NP; ++p) {
       const size_t k = sidx(prm, o, p, j);
       float sp;
-      const float ef = step_bin(prm, P, wi, dts, wdir, ev[u], __bfloat162float(h[o * NP + pr]), o, p, j, sp);
-      P.ES[k] = 0.5f * (ev[u] + ef);
-      if (o >= wi.oc) P.EF[k] = ef;  // as the integration: E* only at propagated levels
+      P.EF[k] = step(p, P.E[k], logl2z, cp0, fkovg, true, sp);
     }
   }
 }
@@ -381,9 +391,10 @@ cudaError_t launch_targets(const Params& prm, const Ptrs& P, const int* pts, int
 
 cudaError_t launch_apply(const Params& prm, const Ptrs& P, const __nv_bfloat16* Y, float tol, float tol_level,
                          unsigned char* fb_pt, int* fb_tile, unsigned long long* counts, cudaStream_t st) {
-  static cudaError_t attr = cudaFuncSetAttribute(k_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_SMEM);
-  if (attr != cudaSuccess) return attr;
-  k_apply<<<prm.NB, 256, TILE_SMEM, st>>>(prm, P, Y, tol, tol_level, fb_pt, fb_tile, counts);
+  // direction cosines [pm][32] and each warp's staged row segments [32][pm|1]
+  const int smem = prm.P * 32 * 4 + 8 * 32 * (prm.P | 1) * 2;
+  if (smem > 48 * 1024 || prm.P % 2) return cudaErrorInvalidConfiguration;
+  k_apply<<<prm.NB, 256, smem, st>>>(prm, P, Y, tol, tol_level, fb_pt, fb_tile, counts);
   return cudaGetLastError();
 }
 
