@@ -814,6 +814,7 @@ def main():
     # timed region: K substeps, inner loop as a CUDA graph (no host round trip per substep)
     U.set_option("use_graph", 1)
     launches0 = U.stat("launches")
+    pstage0 = [U.stat("persistent_stage:%d" % n) for n in range(7)]
     clocks = Clocks(local_rank)
     dist.barrier()
     clocks.start()
@@ -828,6 +829,11 @@ def main():
     clk = clocks.stop()
     launches = int(U.stat("launches") - launches0)
     nsteps = U.dims()["substeps"] - sub0
+    # the persistent kernel's stages (block 0's view, incl. the barrier that ends each)
+    pstage = {name: (U.stat("persistent_stage:%d" % n) - pstage0[n]) / max(nsteps, 1)
+              for n, name in enumerate(("forcing", "sea_ice", "dts_prepass", "dts", "integration", "propagation",
+                                        "screen"))}
+    pstage = pstage if sum(pstage.values()) > 0 else None
     # per-kernel CUDA-event durations: the same K substeps again, host-driven
     # loop with an event pair around every launch
     U.set_option("use_graph", 0)
@@ -899,7 +905,7 @@ def main():
                        "wet_points": N, "bins_per_point": BINS, "replicas": world, "autotune": tune},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clk, "kernel_ms_per_step": {k: kms[k] / max(nsteps, 1) for k in kms if kms[k] > 0},
-            "wall_ms_per_step": wall * 1e3 / nsteps,
+            "wall_ms_per_step": wall * 1e3 / nsteps, "persistent_stage_ms_per_step": pstage,
             "kernel_timed_ms_per_step": kt_ms / max(nsteps, 1),
             "timing": "value: CUDA events around K substeps run as a graph-driven inner loop; roofline and "
                       "kernel_ms_per_step: per-launch CUDA events over K further substeps (host-driven loop)"}

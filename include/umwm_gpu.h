@@ -224,8 +224,16 @@ int umwm_gpu_get_screen(double* out, long n, long* rows);
  * which changes results by rounding only; choices are cached per domain
  * shape for the life of the process), "count_cut" (1: count the bins
  * whose negative ef the propagation cuts to 0 before e = ef, read with
- * umwm_gpu_get_stat "cut_count"; pm = 36 only).  This library's own options
- * have no counterpart in the reference. */
+ * umwm_gpu_get_stat "cut_count"; pm = 36 only), "persistent" (1: each
+ * dtg's inner loop, every member, runs as one cooperative launch of the
+ * persistent substep kernel with grid barriers between the stages; each
+ * barrier wait is bounded (2 s) and one that runs out ends the run with
+ * UMWM_ERR_TIMEOUT; pm = 36 and one direction mapping for all kernels;
+ * results are bit-identical to the other loops), "persistent_stall_test"
+ * (1: the next persistent launch's barrier expects one CTA more than
+ * launched, so its waits run out after 20 ms: for testing the time-out
+ * path).  This library's own options have no counterpart in the
+ * reference. */
 int umwm_gpu_set_option(const char* name, double value);
 
 /* Run statistics: "substeps", "gpu_ms" (device time of the last run),
@@ -235,7 +243,11 @@ int umwm_gpu_set_option(const char* name, double value);
  * "count_cut" was set), "autotune_active", "autotune_done",
  * "autotune_substeps" (substeps measured),
  * "config:phys" / "config:integ" / "config:advect" (launch configuration in
- * use: direction groups * 100 + CTAs per SM * 10 + prefetch levels). */
+ * use: direction groups * 100 + CTAs per SM * 10 + prefetch levels),
+ * "tune_n:<kernel>", "tune_cfg:<kernel>:<i>", "tune_ms:<kernel>:<i>" (the
+ * autotuner's candidates, their configurations and median times),
+ * "persistent_graph" (1: the persistent launch is captured in a CUDA graph,
+ * -1: launched directly, 0: not run yet). */
 double umwm_gpu_get_stat(const char* name);
 
 /* Message of the last failure ("" if none). */

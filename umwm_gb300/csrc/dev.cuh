@@ -143,6 +143,11 @@ struct Global {
   // and the error flag a timed-out wait sets (reset before each launch)
   unsigned bar_count, bar_gen;
   int bar_err;
+  // time block 0 of the persistent kernel spent in each stage, up to and
+  // including the barrier that ends it (globaltimer ns, accumulated over
+  // launches until read): forcing, sea ice, dts pre-pass, dts, integration,
+  // propagation, screen
+  unsigned long long stage_ns[8];
 };
 
 struct Ptrs {

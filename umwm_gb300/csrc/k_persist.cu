@@ -78,7 +78,17 @@ __global__ void __launch_bounds__(128, 4)
   const int nb = gridDim.x;
   const int compute_rot = prm.currents;
   Global* gl = P.glob;
-  auto bar = [&] { return grid_barrier(gl, expected, limit_ns, &ok_s); };
+  // each barrier ends a stage; block 0 books the stage's time
+  unsigned long long t_last = globaltimer_ns();
+  auto bar_s = [&](int stage) {
+    const bool ok = grid_barrier(gl, expected, limit_ns, &ok_s);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      const unsigned long long t = globaltimer_ns();
+      gl->stage_ns[stage] += t - t_last;
+      t_last = t;
+    }
+    return ok;
+  };
   const int budget = gl->budget;  // armed before the launch (k_loop_arm)
   for (int it = 0; it < budget; ++it) {
     // forcing interpolation of every member still inside the dtg
@@ -88,15 +98,15 @@ __global__ void __launch_bounds__(128, 4)
       if (ctl->done) continue;
       for (int i = blockIdx.x * 128 + threadIdx.x; i < M.NM; i += nb * 128) prep_point(prm, P, M, ctl, i, compute_rot);
     }
-    if (!bar()) return;
+    if (!bar_s(0)) return;
     if (prm.ice_possible) {
       for (int j = blockIdx.x * 128 + threadIdx.x; j < prm.Ntot; j += nb * 128) sice_point(prm, P, j);
-      if (!bar()) return;
+      if (!bar_s(1)) return;
     }
     for (int v = blockIdx.x; v < nvb; v += nb) source_body<G, H, false, false>(prm, P, compute_rot, v, sm.phys);
-    if (!bar()) return;
+    if (!bar_s(2)) return;
     if (blockIdx.x == 0) dts_body(prm, P, compute_rot, 0);
-    if (!bar()) return;
+    if (!bar_s(3)) return;
     for (int v = blockIdx.x; v < nvb; v += nb) {
       const Ctl* ctl = prm.mem[prm.tile_mem[(v * PPC) / TILE]].ctl;
       if (P.src_sin && (ctl->done || ctl->first) && gl->save_src)
@@ -104,12 +114,12 @@ __global__ void __launch_bounds__(128, 4)
       else
         source_body<G, H, true, false>(prm, P, 0, v, sm.integ);
     }
-    if (!bar()) return;
+    if (!bar_s(4)) return;
     for (int v = blockIdx.x; v < nvb; v += nb) advect_body<G, H, CURV, false, true>(prm, P, v, sm.adv);
-    if (!bar()) return;
+    if (!bar_s(5)) return;
     for (int m = blockIdx.x; m < prm.nmem; m += nb) screen_member<256, 128>(prm, P, m, sm.scr[0], sm.scr[1]);
     if (blockIdx.x == 0 && threadIdx.x == 0) gl->iters += 1;
-    if (!bar()) return;
+    if (!bar_s(6)) return;
     // not_done was set by this substep's dts, two barriers ago
     if (*(volatile int*)&gl->not_done == 0) break;
   }

@@ -2234,6 +2234,13 @@ double umwm_gpu_get_stat(const char* name) {
   if (s == "bin_updates") return M->last_bins;
   if (s == "launches") return (double)M->launches;
   if (s == "persistent_graph") return (double)M->pgraph_state;  // 1 captured, -1 direct launches, 0 not run
+  if (s.compare(0, 17, "persistent_stage:") == 0) {  // ms block 0 spent in stage n of the persistent kernel
+    const int n = std::atoi(s.c_str() + 17);
+    if (n < 0 || n >= 8) return -1.0;
+    unsigned long long v = 0;
+    if (cudaMemcpy(&v, &M->d_glob->stage_ns[n], sizeof v, cudaMemcpyDeviceToHost) != cudaSuccess) return -1.0;
+    return (double)v * 1e-6;
+  }
   if (s == "cut_count") {  // bins the non-negativity cut changed since count_cut was set
     unsigned long long c = 0;
     if (cudaMemcpy(&c, &M->d_glob->cut_count, sizeof c, cudaMemcpyDeviceToHost) != cudaSuccess) return -1.0;
