@@ -306,7 +306,7 @@ def run_ensemble(args):
         seq_bins += U.stat("bin_updates")
         seq_sub += U.dims()["substeps"] - s0
         seq_ht.append((k, U.get_field("ht")))
-        seq_groups.add(int(U.stat("config:integ")) // 100)
+        seq_groups.add((int(U.stat("config:integ")) // 100) % 10)
         U.umwm_finalize()
     t_seq = time.perf_counter() - t_seq
 
@@ -323,7 +323,7 @@ def run_ensemble(args):
         U.set_option("autotune", args.autotune)
     k = warm(args.autotune)
     tune = {kk: int(U.stat("config:" + kk)) for kk in ("phys", "integ", "advect")} if args.autotune else None
-    bat_groups = int(U.stat("config:integ")) // 100
+    bat_groups = (int(U.stat("config:integ")) // 100) % 10
     launches0 = U.stat("launches")
     clocks = Clocks(local_rank)
     clocks.start()
@@ -801,8 +801,9 @@ def main():
             advance_to(U.dims()["substeps"] + 1)
         cfg = {k: int(U.stat("config:" + k)) for k in ("phys", "integ", "advect")}
         tune = {"mode": args.autotune, "substeps_measured": int(U.stat("autotune_substeps")),
-                "choice": {k: {"direction_groups": v // 100, "ctas_per_sm": (v // 10) % 10 or "default",
-                               "prefetch_levels": v % 10} for k, v in cfg.items()},
+                "choice": {k: {"direction_groups": (v // 100) % 10, "ctas_per_sm": (v // 10) % 10 or "default",
+                               "prefetch_levels": v % 10, "own_rows_by_bulk_copy": bool(v // 1000)}
+                           for k, v in cfg.items()},
                 "median_ms": {k: {str(int(U.stat("tune_cfg:%s:%d" % (k, i)))): round(U.stat("tune_ms:%s:%d" % (k, i)), 4)
                                   for i in range(int(U.stat("tune_n:" + k)))} for k in cfg}}
     case.restart = None  # drop the host copies of the 4.3 GB restart spectrum

@@ -65,3 +65,33 @@ def test_autotune_direction_mapping_parity(lib_built, oracle_mod):
     o = run_oracle(oracle_mod, case, 32, max_substeps=95)
     l2, p999, _ = spec_stats(F, o.get("e"))
     assert l2 < 1e-4 and p999 < 1e-3, (l2, p999)
+
+
+def test_advect_tma_bit_identical(lib_built):
+    """The propagation with its own E* and e rows staged in shared memory by
+    bulk copies (option advect_tma, one of the tuner's candidates) reads the
+    same values as the kernel that loads them from global memory, so the run
+    is bit-identical."""
+    from umwm_gb300 import configs
+
+    U = lib_built
+    case = configs.random_field(mm=96, nm=80, hours=1, dx=2000.0)
+
+    def run(tma):
+        U.clear_inputs()
+        case.stage(U)
+        U.umwm_initialize(nml_text=case.nml)
+        U.set_option("direction_groups", 2)  # the TMA form is the two-group form
+        U.set_option("advect_tma", tma)
+        U.set_option("max_substeps", 12)
+        U.umwm_run(case.start, case.stop)
+        F, u = U.get_state()
+        cfg = U.stat("config:advect")
+        U.umwm_finalize()
+        return F, u, cfg
+
+    F0, u0, c0 = run(0)
+    F1, u1, c1 = run(1)
+    assert c0 < 1000 <= c1
+    np.testing.assert_array_equal(F1, F0)
+    np.testing.assert_array_equal(u1, u0)

@@ -49,13 +49,60 @@ struct AdvSmem {
   float stg[2][ST ? H : 1][128];
 };
 
+// 1-D bulk copies (TMA) into shared memory completing on an mbarrier, and
+// the bounded wait for them (about 2 s of clock)
+__device__ __forceinline__ uint32_t adv_smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void adv_mbar_init(uint32_t bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void adv_mbar_expect(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void adv_bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ bool adv_mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool adv_mbar_wait(uint32_t bar, uint32_t parity, long long limit_cycles) {
+  if (adv_mbar_try(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!adv_mbar_try(bar, parity))
+    if (clock64() - t0 > limit_cycles) return false;
+  return true;
+}
+
+// Own-row staging of the TMA form of the propagation: each level's E* and e
+// rows of the CTA's 64 points (two blocks, one contiguous region per array)
+// land in shared memory by two bulk copies issued one level ahead, into two
+// alternating buffers, each completing on its own mbarrier.
+struct OwnStage {
+  float* buf;     // [2 buffers][2 arrays: E*, e][2 blocks][P][32]
+  uint32_t mbar;  // two mbarriers, 8 bytes apart
+};
+
 // The body of k_advect for CTA tile `cta` (the kernel's block index, or a
 // persistent CTA's current tile).  CNT: also count the bins whose negative ef
 // is cut to 0 (option "count_cut"; a separate instance so that the plain one
 // carries no counter).  COH: E* is read with coherent loads instead of the
 // read-only path, for a persistent kernel in which the same launch wrote it.
-template <int G, int H, bool CURV, bool CNT, bool COH>
-__device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, int cta, AdvSmem<G, H, CURV>& sm) {
+// TMA: the own rows come from shared memory staged by bulk copies (OwnStage;
+// the two-group, plain-grid mapping with rows in halves only).
+template <int G, int H, bool CURV, bool CNT, bool COH, bool TMA = false>
+__device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, int cta, AdvSmem<G, H, CURV>& sm,
+                                            OwnStage own = OwnStage{nullptr, 0u}) {
   constexpr int PW = 32 / G;   // points per warp
   constexpr int PPC = 4 * PW;  // points per CTA (4 warps)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -203,9 +250,60 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
   constexpr bool HV = NPART > 1 && SW && ST && G == 2 && (H % (NPART > 1 ? NPART : 1) == 0);
   const size_t oPt = sidx(prm, 0, 0, jj);  // the point's row 0 (all groups)
   const int pprev = ((q + G - 1) % G) * H + H - 1, pnext = ((q + 1) % G) * H;
+  // TMA: the own rows in shared memory.  jj (the ghost for padding lanes)
+  // lies in this CTA's 64 points: a member's ghost is in its last tile
+  static_assert(!TMA || HV, "the TMA form is the two-group, plain-grid form with rows in halves");
+  const int row = 2 * prm.P * 32;  // floats of one array (two blocks) in a buffer
+  const int jl64 = jj - cta * PPC;
+  const int sS = ((jl64 >> 5) * prm.P + q * H) * 32 + (jl64 & 31);  // the lane's row in a staged array
+  const int sPt = ((jl64 >> 5) * prm.P) * 32 + (jl64 & 31);          // the point's row 0
+  int occ = O;  // levels of which E* is staged: the CTA's largest cut-off
+  const size_t src0 = sidx(prm, 0, 0, cta * PPC);
+  auto issue = [&](int o) {  // one thread: level o's rows into buffer o & 1
+    if (o >= O) return;
+    const int b = o & 1;
+    const uint32_t bar = own.mbar + 8u * b;
+    const uint32_t bytes = (uint32_t)row * 4u;
+    adv_mbar_expect(bar, (o < occ ? 2u : 1u) * bytes);
+    adv_bulk_copy(adv_smem_u32(own.buf + (size_t)(2 * b + 1) * row), P.EF + src0 + (size_t)o * lstride, bytes, bar);
+    if (o < occ) adv_bulk_copy(adv_smem_u32(own.buf + (size_t)(2 * b) * row), P.ES + src0 + (size_t)o * lstride, bytes, bar);
+  };
+  if (TMA) {
+    __shared__ int s_occ;
+    if (threadIdx.x == 0) {
+      s_occ = 0;
+      adv_mbar_init(own.mbar);
+      adv_mbar_init(own.mbar + 8u);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (lane == 0) atomicMax(&s_occ, ocw);
+    __syncthreads();
+    occ = s_occ;
+    if (threadIdx.x == 0) issue(0);
+  }
   for (int o = 0; o < (HV ? O : 0); ++o) {
     pf(o + PFD);
     if (ST) cp_async_wait<0>();  // this level's copies have landed
+    if (TMA) {
+      // this level's own rows have landed (bounded wait: an error flag and
+      // a bounded drain of the other buffer's copy instead of a hang)
+      const bool ok = adv_mbar_wait(own.mbar + 8u * (o & 1), (o >> 1) & 1, 4000000000LL);
+      if (!__syncthreads_and(ok)) {
+        if (threadIdx.x == 0) {
+          atomicOr(&const_cast<Ctl*>(ctl)->err, 2);
+          if (o + 1 < O) adv_mbar_wait(own.mbar + 8u * ((o + 1) & 1), ((o + 1) >> 1) & 1, 400000000LL);
+        }
+        return;
+      }
+      // every thread is done with the other buffer (level o - 1): refill it
+      if (threadIdx.x == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(o + 1);
+      }
+    }
+    const float* ownES = TMA ? own.buf + (size_t)(2 * (o & 1)) * row : nullptr;
+    const float* ownE = TMA ? own.buf + (size_t)(2 * (o & 1) + 1) * row : nullptr;
     constexpr int HH = HV ? H / NPART : 1;
     const float* T = P.TAB + (size_t)o * tstride;
     const float* __restrict__ ESo = P.ES + (size_t)o * lstride;
@@ -246,11 +344,11 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
       const int k0 = h * HH;
       float ef[HH];
 #pragma unroll
-      for (int i = 0; i < HH; ++i) ef[i] = EFo[oS + (k0 + i) * 32];  // e below the cut-off, ef above
+      for (int i = 0; i < HH; ++i) ef[i] = TMA ? ownE[sS + (k0 + i) * 32] : EFo[oS + (k0 + i) * 32];  // e below the cut-off, ef above
       if (prog) {
         float es[HH];
 #pragma unroll
-        for (int i = 0; i < HH; ++i) es[i] = lde(ESo + oS + (k0 + i) * 32);
+        for (int i = 0; i < HH; ++i) es[i] = TMA ? ownES[sS + (k0 + i) * 32] : lde(ESo + oS + (k0 + i) * 32);
 #pragma unroll
         for (int i = 0; i < HH; ++i) ef[i] = 2.f * es[i] - ef[i];  // ef = 2 E* - e
         // ---- propagation, umwm_advection.F90:30-97
@@ -272,8 +370,10 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
         if (refr) {
           // E* beyond this part's edges: the neighbouring parts, or the other
           // group's edge rows
-          const float esL = h == 0 ? lde(ESo + oPt + pprev * 32) : lde(ESo + oS + (k0 - 1) * 32);
-          const float esR = h == NPART - 1 ? lde(ESo + oPt + pnext * 32) : lde(ESo + oS + (k0 + HH) * 32);
+          const float esL = TMA ? (h == 0 ? ownES[sPt + pprev * 32] : ownES[sS + (k0 - 1) * 32])
+                                : (h == 0 ? lde(ESo + oPt + pprev * 32) : lde(ESo + oS + (k0 - 1) * 32));
+          const float esR = TMA ? (h == NPART - 1 ? ownES[sPt + pnext * 32] : ownES[sS + (k0 + HH) * 32])
+                                : (h == NPART - 1 ? lde(ESo + oPt + pnext * 32) : lde(ESo + oS + (k0 + HH) * 32));
 #pragma unroll
           for (int i = 0; i < HH; ++i) {
             const int k = k0 + i;

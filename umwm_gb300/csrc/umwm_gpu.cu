@@ -110,6 +110,7 @@ struct MemberHost {
 // domain signature for the life of the process.
 struct TuneCand {
   int g4, minb, pf;  // quarter-turn groups, CTAs per SM (0: default instance), levels prefetched
+  int tma = 0;       // propagation only: own rows staged by bulk copies (k_advect_tma)
 };
 struct KernelTune {
   std::vector<TuneCand> cands;
@@ -296,12 +297,12 @@ std::string tune_key(const Model& M) {
 TuneCand tune_get(const Params& p, int k) {
   if (k == TK_PHYS) return {p.groups4_phys, p.minb_phys, p.pf_phys};
   if (k == TK_INTEG) return {p.groups4, p.minb_integ, p.pf_integ};
-  return {p.adv_groups4, p.minb_adv, p.pf_adv};
+  return {p.adv_groups4, p.minb_adv, p.pf_adv, p.adv_tma};
 }
 void tune_set(Params& p, int k, const TuneCand& c) {
   if (k == TK_PHYS) { p.groups4_phys = c.g4; p.minb_phys = c.minb; p.pf_phys = c.pf; }
   else if (k == TK_INTEG) { p.groups4 = c.g4; p.minb_integ = c.minb; p.pf_integ = c.pf; }
-  else { p.adv_groups4 = c.g4; p.minb_adv = c.minb; p.pf_adv = c.pf; }
+  else { p.adv_groups4 = c.g4; p.minb_adv = c.minb; p.pf_adv = c.pf; p.adv_tma = c.tma; }
 }
 
 // Candidate lists.  Register budgets have kernel instances only for the
@@ -341,7 +342,10 @@ void tune_start(Model& M, int mode) {
         pfs = {1, 2};
       }
       for (int mb : minbs)
-        for (int pf : pfs) K.cands.push_back({g4, mb, pf});
+        for (int pf : pfs) K.cands.push_back({g4, mb, pf, 0});
+      // the propagation with its own rows staged by bulk copies (3 CTAs per SM)
+      if (k == TK_ADVECT && d36 && !p.curvilinear && !g4)
+        for (int pf : pfs) K.cands.push_back({0, 3, pf, 1});
     }
     K.ms.assign(K.cands.size(), {});
     K.best = -1;
@@ -623,6 +627,7 @@ int setup_params(Model& M) {
   // launch configuration: default register budgets (0) and prefetch distances
   p.minb_phys = p.minb_integ = p.minb_adv = 0;
   p.count_cut = 0;
+  p.adv_tma = 0;
   p.pf_phys = UMWM_PF_DIST_PHYS;
   p.pf_integ = UMWM_PF_DIST_INTEG;
   p.pf_adv = UMWM_PF_DIST_ADV;
@@ -2207,6 +2212,11 @@ int umwm_gpu_set_option(const char* name, double value) {
       return UMWM_OK;
     }
   }
+  if (s == "advect_tma") {  // the propagation's own rows staged by bulk copies (two-group plain grids, pm 36)
+    M->prm.adv_tma = value != 0 ? 1 : 0;
+    drop_graph(*M);
+    return UMWM_OK;
+  }
   if (s == "count_cut") {
     if (value != 0 && M->prm.P != 36)
       return fail(UMWM_ERR_UNSUPPORTED, "count_cut needs pm = 36 (the counting kernel instances)");
@@ -2260,7 +2270,8 @@ double umwm_gpu_get_stat(const char* name) {
     if (what == "tune_n") return (double)K.cands.size();
     const int i = c2 == std::string::npos ? -1 : std::atoi(s.c_str() + c2 + 1);
     if (i < 0 || i >= (int)K.cands.size()) return -1.0;
-    if (what == "tune_cfg") return (K.cands[i].g4 ? 4 : 2) * 100.0 + K.cands[i].minb * 10.0 + K.cands[i].pf;
+    if (what == "tune_cfg")
+      return K.cands[i].tma * 1000.0 + (K.cands[i].g4 ? 4 : 2) * 100.0 + K.cands[i].minb * 10.0 + K.cands[i].pf;
     if (what == "tune_ms") {
       std::vector<float> v = K.ms[i];
       if (v.empty()) return -1.0;
@@ -2277,7 +2288,7 @@ double umwm_gpu_get_stat(const char* name) {
   if (s == "config:phys" || s == "config:integ" || s == "config:advect") {
     const int k = s == "config:phys" ? TK_PHYS : s == "config:integ" ? TK_INTEG : TK_ADVECT;
     const TuneCand c = tune_get(M->prm, k);
-    return (c.g4 ? 4 : 2) * 100.0 + c.minb * 10.0 + c.pf;
+    return c.tma * 1000.0 + (c.g4 ? 4 : 2) * 100.0 + c.minb * 10.0 + c.pf;
   }
   if (s == "device_free_bytes") {  // cudaMemGetInfo of the current device
     size_t fr = 0, tot = 0;
