@@ -11,7 +11,9 @@ of the restatement in oracle/umwm_oracle.cpp:
   secant slopes over [x1, x2], and exponential decay from its value at x2;
 * Sds of a two-bin spectrum (umwm_source_functions.F90:85-105, :174-176): the
   mean-square-slope factor of the upper bin is (1 + mss_fac E1 cos^2(dtheta)
-  dth k^3 dk)^2 from the lower bin alone;
+  dth k^3 dk)^2 from the lower bin alone; and its Snl (:156-171): each bin
+  loses snl_fac Sds e and hands the renormalised bf1, bf2 shares one and two
+  levels down;
 * the monochromatic deep-water Stokes drift u_s(z) = omega k a^2 e^{2kz}
   (umwm_stokes.F90:55-101) summed over the bins of the spectrum, with a^2
   twice each bin's variance, and the e-folding depth 1/(2k) below the first
@@ -208,6 +210,70 @@ def test_sds_two_bins_gpu(lib_built):
     U.umwm_finalize()
     np.testing.assert_allclose(sds[:, P1, O1], s_lo, rtol=1e-4)
     np.testing.assert_allclose(sds[:, P2, O2], s_hi, rtol=1e-4)
+
+
+def snl_expected(om=37):
+    """Snl of the two-bin spectrum (umwm_source_functions.F90:156-171): each
+    energetic bin o loses snl_fac Sds(o) e(o) and passes the shares bf1 and
+    bf2 of it, times kdk(o)/kdk(o-1) and kdk(o)/kdk(o-2), down one and two
+    levels, with bf1 : bf2 = exp(-16 dlnf^2) : exp(-64 dlnf^2) normalised to
+    a sum of 1 (umwm_init.F90:1290-1294), so the energy sum(kdk Snl) is
+    conserved; Sds before the coth factor.  Returns ({(o, p): Snl}, kdk)."""
+    f, dlnf = freqs(om)
+    s_lo, s_hi, _ = sds_expected(om)
+    coth = lambda k: 1.0 / np.tanh(0.2 * min(k * SDS_DEPTH, 20.0))
+    k = np.array([exact_k(x, SDS_DEPTH) for x in f])
+    kdk = k * 2 * np.pi * f * dlnf / np.array([exact_cg(x, SDS_DEPTH) for x in k])
+    b1, b2 = np.exp(-16 * dlnf ** 2), np.exp(-64 * dlnf ** 2)
+    bf1, bf2 = b1 / (b1 + b2), b2 / (b1 + b2)
+    out = {}
+    for o, p, e, sds in ((O1, P1, E1, s_lo / coth(k[O1])), (O2, P2, E2, s_hi / coth(k[O2]))):
+        loss = 5.0 * sds * e  # snl_fac = 5
+        out[(o, p)] = out.get((o, p), 0.0) - loss
+        out[(o - 1, p)] = out.get((o - 1, p), 0.0) + bf1 * kdk[o] / kdk[o - 1] * loss
+        out[(o - 2, p)] = out.get((o - 2, p), 0.0) + bf2 * kdk[o] / kdk[o - 2] * loss
+    return out, kdk
+
+
+def _check_snl(snl):
+    exp, kdk = snl_expected()
+    top = max(abs(v) for v in exp.values())
+    for (o, p), v in exp.items():
+        np.testing.assert_allclose(snl[:, p, o], v, rtol=2e-4, atol=1e-6 * top)
+    # the downshifting conserves energy: sum over o of kdk Snl is zero
+    for p in (P1, P2):
+        cons = np.abs((snl[:, p, :] * kdk[None, :]).sum(axis=1))
+        assert cons.max() <= 1e-4 * max(abs(v) * kdk[o] for (o, pp), v in exp.items() if pp == p)
+    # no other bin of the two directions sees the downshifting
+    for p in (P1, P2):
+        others = [o for o in range(37) if (o, p) not in exp]
+        assert np.abs(snl[:, p, others]).max() <= 1e-6 * top
+
+
+def test_snl_two_bins_oracle(oracle_mod):
+    case = _two_bin_case()
+    for prec in (32, 64):
+        o = oracle_mod.Oracle(case.nml, prec)
+        case.stage(o)
+        o.initialize()
+        o.set_option("max_substeps", 1)
+        o.run(case.start, case.stop)
+        _check_snl(o.get("snl"))
+
+
+@pytest.mark.gpu
+def test_snl_two_bins_gpu(lib_built):
+    U = lib_built
+    case = _two_bin_case()
+    U.clear_inputs()
+    case.stage(U)
+    U.umwm_initialize(nml_text=case.nml)
+    U.set_option("stress_ocn", 1)        # keep the substep's source terms
+    U.set_option("max_substeps", 1)
+    U.umwm_run(case.start, case.stop)
+    snl = U.get_field("snl")
+    U.umwm_finalize()
+    _check_snl(snl)
 
 
 # ---------------------------------------------------------------------------
