@@ -19,7 +19,9 @@ of the restatement in oracle/umwm_oracle.cpp:
   twice each bin's variance, and the e-folding depth 1/(2k) below the first
   level (umwm_stokes.F90:104-128);
 * the unrolling of a periodic (global) grid worked out by hand
-  (umwm_init.F90:897-1007).
+  (umwm_init.F90:897-1007);
+* one first-order upwind step of a step function in x: the front cell gets
+  CFL times the upstream energy (umwm_advection.F90:30-97).
 
 CPU tests run the oracle and the library's host set-up; the GPU tests
 (marked gpu) run the same cases through the CUDA path."""
@@ -400,3 +402,65 @@ def test_known_answer_global_unrolling_library(lib_built):
     assert np.array_equal(U.get_field_i("ii"), KG_II)
     for k, v in list(KG_TRUE.items()) + list(KG_ALIAS.items()):
         assert list(U.get_field_i(k)[:8]) == v, k
+
+
+# ---------------------------------------------------------------------------
+# first-order upwind propagation of a step in x
+# ---------------------------------------------------------------------------
+PR_MM, PR_NM, PR_DX, PR_DEPTH = 20, 8, 5000.0, 1000.0
+PR_O, PR_P, PR_E0, PR_M0 = 2, 17, 1.0, 10  # f ~ 0.039 Hz, theta = -5 degrees
+
+
+def _step_case():
+    """Energy E0 in one bin (deep water, theta = -5 deg) for m <= M0 and
+    tiny(e) elsewhere; no wind (wspd clamped to 0.01), no currents, uniform
+    depth: the sources change the bin by about 1e-6 in a substep and the
+    rotation is zero, so one substep is the textbook upwind step
+    e'(m) = e(m) - dts cg cos(theta) / dx (e(m) - e(m-1))
+    (umwm_advection.F90:30-97 with cge = (cg0_i + cg0_ie) cos th, summed as
+    0.25 dta / ar times the face fluxes)."""
+    from umwm_gb300 import configs
+
+    case = configs.fetch_limited(mm=PR_MM, nm=PR_NM, hours=1, dx=PR_DX, depth=PR_DEPTH, wspd=0.0)
+    t, F, u = case.restart
+    F = np.full_like(F, np.finfo(np.float32).tiny)
+    nw = PR_NM - 2
+    for m in range(2, PR_M0 + 1):
+        F[(m - 2) * nw:(m - 1) * nw, PR_P, PR_O] = PR_E0
+    case.restart = (t, F, np.full_like(u, 1e-3))
+    return case
+
+
+def _check_step(F, dts):
+    f, _ = freqs()
+    th = (PR_P + 1 - 0.5 * 37) * (2 * np.pi / 36)
+    cfl = dts * exact_cg(exact_k(f[PR_O], PR_DEPTH), PR_DEPTH) * np.cos(th) / PR_DX
+    assert 0.3 < cfl < 1.0
+    nw = PR_NM - 2
+    col = lambda m: F[(m - 2) * nw + 2:(m - 1) * nw - 2, PR_P, PR_O]  # interior rows
+    np.testing.assert_allclose(col(PR_M0), PR_E0, rtol=1e-4)          # upstream: unchanged
+    np.testing.assert_allclose(col(PR_M0 + 1), cfl * PR_E0, rtol=1e-4)  # the front advances by CFL
+    assert col(PR_M0 + 2).max() < 1e-30                                 # nothing beyond it
+
+
+def test_upwind_step_oracle(oracle_mod):
+    case = _step_case()
+    for prec in (32, 64):
+        o = oracle_mod.Oracle(case.nml, prec)
+        case.stage(o)
+        o.initialize()
+        o.set_option("max_substeps", 1)
+        o.run(case.start, case.stop)
+        _check_step(o.get("e"), o.scalar("dts"))
+
+
+@pytest.mark.gpu
+def test_upwind_step_gpu(lib_built):
+    from helpers import run_gpu
+
+    U = lib_built
+    run_gpu(U, _step_case(), max_substeps=1)
+    F, _ = U.get_state()
+    dts = U.get_field("dts")
+    U.umwm_finalize()
+    _check_step(F, dts)
