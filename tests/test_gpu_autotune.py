@@ -5,7 +5,9 @@ Mode 1 tunes the register budget (resident CTAs per SM) and the L2 prefetch
 distance of the dts pre-pass, the integration and the propagation while the
 model's own substeps run, round-robin over the candidates, five samples each.  Neither knob
 changes any arithmetic, so a tuned run is compared bit for bit with an untuned
-one, also across the substeps during which the candidates rotate.  Mode 2
+one, also across the substeps during which the candidates rotate (the
+candidates include the forms of the propagation and the dts pre-pass that
+stage their own rows with bulk copies).  Mode 2
 also tunes the direction mapping, which changes summation order only: its run
 meets the oracle's parity bar.  The choice is cached per domain signature, so
 a second model of the same shape starts tuned.
@@ -47,7 +49,7 @@ def test_autotune_bit_identical(lib_built):
     # 9 pre-pass candidates x 5 samples after the first substep: tuning done
     assert info["done"] == 1 and info["active"] == 0 and info["measured"] == 45
     for c in info["config"]:
-        assert int(c) // 100 in (2, 4) and 1 <= int(c) % 10 <= 3
+        assert (int(c) // 100) % 10 in (2, 4) and 1 <= int(c) % 10 <= 3
     # the same shape again starts from the cached choice
     F2, u2, info2 = _run(U, case, 1, 50)
     assert info2["done"] == 1 and info2["measured"] == 0 and info2["config"] == info["config"]
@@ -59,19 +61,21 @@ def test_autotune_direction_mapping_parity(lib_built, oracle_mod):
 
     U = lib_built
     case = configs.random_field(mm=48, nm=40, hours=2, dx=2000.0)
-    # 18 pre-pass candidates (two mappings) x 5 samples after the first substep
-    F, _, info = _run(U, case, 2, 95)
-    assert info["done"] == 1 and info["measured"] == 90
-    o = run_oracle(oracle_mod, case, 32, max_substeps=95)
+    # 20 pre-pass candidates (two mappings, two with staged rows) x 5 samples
+    # after the first substep
+    F, _, info = _run(U, case, 2, 110)
+    assert info["done"] == 1 and info["measured"] == 100
+    o = run_oracle(oracle_mod, case, 32, max_substeps=110)
     l2, p999, _ = spec_stats(F, o.get("e"))
     assert l2 < 1e-4 and p999 < 1e-3, (l2, p999)
 
 
-def test_advect_tma_bit_identical(lib_built):
-    """The propagation with its own E* and e rows staged in shared memory by
-    bulk copies (option advect_tma, one of the tuner's candidates) reads the
-    same values as the kernel that loads them from global memory, so the run
-    is bit-identical."""
+@pytest.mark.parametrize("option", ["advect_tma", "phys_tma"])
+def test_tma_forms_bit_identical(lib_built, option):
+    """The propagation and the dts pre-pass with their own rows staged in
+    shared memory by bulk copies (options advect_tma, phys_tma; candidates of
+    the tuner) read the same values as the kernels that load them from
+    global memory, so the run is bit-identical."""
     from umwm_gb300 import configs
 
     U = lib_built
@@ -82,11 +86,11 @@ def test_advect_tma_bit_identical(lib_built):
         case.stage(U)
         U.umwm_initialize(nml_text=case.nml)
         U.set_option("direction_groups", 2)  # the TMA form is the two-group form
-        U.set_option("advect_tma", tma)
+        U.set_option(option, tma)
         U.set_option("max_substeps", 12)
         U.umwm_run(case.start, case.stop)
         F, u = U.get_state()
-        cfg = U.stat("config:advect")
+        cfg = U.stat("config:advect" if option == "advect_tma" else "config:phys")
         U.umwm_finalize()
         return F, u, cfg
 

@@ -49,50 +49,6 @@ struct AdvSmem {
   float stg[2][ST ? H : 1][128];
 };
 
-// 1-D bulk copies (TMA) into shared memory completing on an mbarrier, and
-// the bounded wait for them (about 2 s of clock)
-__device__ __forceinline__ uint32_t adv_smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void adv_mbar_init(uint32_t bar) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void adv_mbar_expect(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void adv_bulk_copy(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(bar)
-               : "memory");
-}
-__device__ __forceinline__ bool adv_mbar_try(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-__device__ __forceinline__ bool adv_mbar_wait(uint32_t bar, uint32_t parity, long long limit_cycles) {
-  if (adv_mbar_try(bar, parity)) return true;
-  const long long t0 = clock64();
-  while (!adv_mbar_try(bar, parity))
-    if (clock64() - t0 > limit_cycles) return false;
-  return true;
-}
-
-// Own-row staging of the TMA form of the propagation: each level's E* and e
-// rows of the CTA's 64 points (two blocks, one contiguous region per array)
-// land in shared memory by two bulk copies issued one level ahead, into two
-// alternating buffers, each completing on its own mbarrier.
-struct OwnStage {
-  float* buf;     // [2 buffers][2 arrays: E*, e][2 blocks][P][32]
-  uint32_t mbar;  // two mbarriers, 8 bytes apart
-};
-
 // The body of k_advect for CTA tile `cta` (the kernel's block index, or a
 // persistent CTA's current tile).  CNT: also count the bins whose negative ef
 // is cut to 0 (option "count_cut"; a separate instance so that the plain one

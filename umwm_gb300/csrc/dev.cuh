@@ -94,6 +94,7 @@ struct Params {
   int pf_phys, pf_integ, pf_adv;
   int count_cut;     // the propagation counts the bins its non-negativity cut changes (Global::cut_count)
   int adv_tma;       // the propagation stages its own rows with bulk copies (k_advect_tma; option "advect_tma")
+  int phys_tma;      // the dts pre-pass does (k_source_tma; option "phys_tma")
   float f[MAX_OM], dom[MAX_OM];
   float th[MAX_PM], cth[MAX_PM], sth[MAX_PM], c2th[MAX_PM], s2th[MAX_PM];
   // max(cos th, 0), min(cos th, 0), max(sin th, 0), min(sin th, 0): the

@@ -60,6 +60,18 @@ __global__ void __launch_bounds__(128, MINB) k_source(const Params prm, const Pt
   source_body<G, H, INTEG, false>(prm, P, compute_rot, blockIdx.x, sm);
 }
 
+// k_source_tma: the dts pre-pass with its own e rows staged in shared memory
+// by bulk copies (OwnStage), for the two-group mapping; 5 CTAs per SM.
+template <int G, int H>
+__global__ void __launch_bounds__(128, 5) k_source_tma(const Params prm, const Ptrs P, int compute_rot) {
+  extern __shared__ __align__(128) unsigned char dsm[];
+  __shared__ __align__(8) unsigned long long mbar[2];
+  auto& sm = *reinterpret_cast<SrcSmem<G, H, false>*>(dsm);
+  constexpr size_t off = (sizeof(SrcSmem<G, H, false>) + 127) & ~size_t(127);
+  const OwnStage own{reinterpret_cast<float*>(dsm + off), adv_smem_u32(mbar)};
+  source_body<G, H, false, false, true>(prm, P, compute_rot, blockIdx.x, sm, own);
+}
+
 // Launch with the register budget of `minb` resident CTAs per SM.  The
 // 36-direction mappings (the configured workloads) have instances for the
 // budgets the autotuner tries (the integration's shared memory allows at
@@ -75,6 +87,15 @@ static void launch_src(int minb, dim3 grid, const Params& prm, const Ptrs& P, in
   if constexpr (G == 2 && H == 18 && INTEG) {
     switch (minb) { INST(3) INST(4) default: break; }
   } else if constexpr (G == 2 && H == 18) {
+    if (prm.phys_tma) {
+      const size_t smem = ((sizeof(SrcSmem<2, 18, false>) + 127) & ~size_t(127)) + (size_t)2 * 2 * prm.P * 32 * 4;
+      static const cudaError_t attr =
+          cudaFuncSetAttribute(k_source_tma<2, 18>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (attr == cudaSuccess) {
+        k_source_tma<2, 18><<<grid, block, smem, st>>>(prm, P, compute_rot);
+        return;
+      }
+    }
     switch (minb) { INST(5) INST(6) INST(7) default: break; }
   } else if constexpr (G == 4 && H == 9) {
     switch (minb) { INST(3) INST(4) INST(5) INST(6) default: break; }

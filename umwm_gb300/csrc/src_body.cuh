@@ -83,9 +83,12 @@ struct SrcSmem {
 // persistent CTA's current tile).  SAVE (integration only): this substep also stores
 // its source terms for stress('ocn'); a separate instantiation, so that the
 // substeps that store nothing carry no predicated stores.
-template <int G, int H, bool INTEG, bool SAVE>
+// TMA (dts pre-pass, two groups): the own e rows come from shared memory,
+// staged one level ahead by bulk copies (OwnStage, one array per buffer).
+template <int G, int H, bool INTEG, bool SAVE, bool TMA = false>
 __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, int compute_rot, int bx,
-                                            SrcSmem<G, H, INTEG>& sm) {
+                                            SrcSmem<G, H, INTEG>& sm, OwnStage own = OwnStage{nullptr, 0u}) {
+  static_assert(!TMA || (!INTEG && G == 2), "the TMA form is the two-group dts pre-pass");
   constexpr int PW = 32 / G;   // points per warp
   constexpr int PPC = 4 * PW;  // points per CTA (4 warps)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -173,13 +176,59 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
 #define LAG_S2(k) (SL ? lag[o & 1][1][SL ? (k) : 0][threadIdx.x] : s2[SL ? 0 : (k)])
   Coef Cc{}, C1{}, C2{};
 
-  const int OL = INTEG ? O + 2 : OP;
+  int OL = INTEG ? O + 2 : OP;
+  // TMA: the CTA's two blocks of e at level o in buffer o & 1; every warp
+  // walks to the CTA's largest cut-off (levels above a lane's own add
+  // nothing to its max).  jj (the ghost for padding lanes) lies in this
+  // CTA's 64 points: a member's ghost is in its last tile
+  const int row = 2 * prm.P * 32;
+  const int jl64 = jj - bx * PPC;
+  const int sS = ((jl64 >> 5) * prm.P + q * H) * 32 + (jl64 & 31);
+  const size_t src0 = sidx(prm, 0, 0, bx * PPC);
+  auto issue = [&](int o) {  // one thread
+    if (o >= OL) return;
+    const uint32_t bar = own.mbar + 8u * (o & 1);
+    adv_mbar_expect(bar, (uint32_t)row * 4u);
+    adv_bulk_copy(adv_smem_u32(own.buf + (size_t)(o & 1) * row), P.E + src0 + (size_t)o * lstride, (uint32_t)row * 4u,
+                  bar);
+  };
+  if (TMA) {
+    __shared__ int s_ol;
+    if (threadIdx.x == 0) {
+      s_ol = 0;
+      adv_mbar_init(own.mbar);
+      adv_mbar_init(own.mbar + 8u);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (lane == 0) atomicMax(&s_ol, OL);
+    __syncthreads();
+    OL = s_ol;
+    if (threadIdx.x == 0) issue(0);
+  }
   for (int o = 0; o < OL; ++o) {
     pf(o + PFD);
+    if (TMA) {
+      // this level's rows have landed (bounded: an error flag and a bounded
+      // drain of the other buffer's copy instead of a hang)
+      const bool ok = adv_mbar_wait(own.mbar + 8u * (o & 1), (o >> 1) & 1, 4000000000LL);
+      if (!__syncthreads_and(ok)) {
+        if (threadIdx.x == 0) {
+          atomicOr(&ctl->err, 2);
+          if (o + 1 < OL) adv_mbar_wait(own.mbar + 8u * ((o + 1) & 1), ((o + 1) >> 1) & 1, 400000000LL);
+        }
+        return;
+      }
+      if (threadIdx.x == 0) {  // every thread is done with the other buffer
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue(o + 1);
+      }
+    }
     if (o < O) {
       const float* r = Eb + (size_t)o * lstride;
+      const float* rs = TMA ? own.buf + (size_t)(o & 1) * row + sS : r;
 #pragma unroll
-      for (int k = 0; k < H; ++k) ec[k] = r[k * 32];  // E is also written (as ef) by this kernel
+      for (int k = 0; k < H; ++k) ec[k] = rs[k * 32];  // E is also written (as ef) by the integration
       const bool prog = o < wi.oc;
       const Level<H> Lc = load_level<H>(prm, Tb + (size_t)o * tstride, !INTEG && prog);
       // the group's cos/sin 2th sign folded into the coefficients

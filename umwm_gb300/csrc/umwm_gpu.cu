@@ -295,12 +295,12 @@ std::string tune_key(const Model& M) {
 
 // the launch configuration of kernel k in M.prm
 TuneCand tune_get(const Params& p, int k) {
-  if (k == TK_PHYS) return {p.groups4_phys, p.minb_phys, p.pf_phys};
+  if (k == TK_PHYS) return {p.groups4_phys, p.minb_phys, p.pf_phys, p.phys_tma};
   if (k == TK_INTEG) return {p.groups4, p.minb_integ, p.pf_integ};
   return {p.adv_groups4, p.minb_adv, p.pf_adv, p.adv_tma};
 }
 void tune_set(Params& p, int k, const TuneCand& c) {
-  if (k == TK_PHYS) { p.groups4_phys = c.g4; p.minb_phys = c.minb; p.pf_phys = c.pf; }
+  if (k == TK_PHYS) { p.groups4_phys = c.g4; p.minb_phys = c.minb; p.pf_phys = c.pf; p.phys_tma = c.tma; }
   else if (k == TK_INTEG) { p.groups4 = c.g4; p.minb_integ = c.minb; p.pf_integ = c.pf; }
   else { p.adv_groups4 = c.g4; p.minb_adv = c.minb; p.pf_adv = c.pf; p.adv_tma = c.tma; }
 }
@@ -343,9 +343,12 @@ void tune_start(Model& M, int mode) {
       }
       for (int mb : minbs)
         for (int pf : pfs) K.cands.push_back({g4, mb, pf, 0});
-      // the propagation with its own rows staged by bulk copies (3 CTAs per SM)
+      // the propagation (3 CTAs per SM) and the dts pre-pass (5) with their
+      // own rows staged by bulk copies
       if (k == TK_ADVECT && d36 && !p.curvilinear && !g4)
         for (int pf : pfs) K.cands.push_back({0, 3, pf, 1});
+      if (k == TK_PHYS && d36 && !g4)
+        for (int pf : {1, 2}) K.cands.push_back({0, 5, pf, 1});
     }
     K.ms.assign(K.cands.size(), {});
     K.best = -1;
@@ -628,6 +631,7 @@ int setup_params(Model& M) {
   p.minb_phys = p.minb_integ = p.minb_adv = 0;
   p.count_cut = 0;
   p.adv_tma = 0;
+  p.phys_tma = 0;
   p.pf_phys = UMWM_PF_DIST_PHYS;
   p.pf_integ = UMWM_PF_DIST_INTEG;
   p.pf_adv = UMWM_PF_DIST_ADV;
@@ -2212,8 +2216,8 @@ int umwm_gpu_set_option(const char* name, double value) {
       return UMWM_OK;
     }
   }
-  if (s == "advect_tma") {  // the propagation's own rows staged by bulk copies (two-group plain grids, pm 36)
-    M->prm.adv_tma = value != 0 ? 1 : 0;
+  if (s == "advect_tma" || s == "phys_tma") {  // own rows staged by bulk copies (two groups, pm 36)
+    (s == "advect_tma" ? M->prm.adv_tma : M->prm.phys_tma) = value != 0 ? 1 : 0;
     drop_graph(*M);
     return UMWM_OK;
   }
