@@ -176,6 +176,15 @@ def make_case(name, size):
         return configs.hurricane(mm=size, nm=size, hours=12, seed=3)
     if name == "fetch_limited":
         return configs.fetch_limited(mm=size, nm=size, hours=6)
+    if name == "curvilinear":
+        # the random field on a skewed longitude/latitude grid (0.02 degrees,
+        # about 2 km): the curvilinear propagation form
+        case = configs.random_field(mm=size, nm=size, hours=3, gridFromFile=True)
+        m = np.arange(size)[:, None]
+        n = np.arange(size)[None, :]
+        case.gridtopo["lon"] = (-80.0 + 0.02 * m + 0.0008 * n).astype(np.float32)
+        case.gridtopo["lat"] = (10.0 + 0.02 * n + 0.0004 * m).astype(np.float32)
+        return case
     return configs.random_field(mm=size, nm=size, hours=3)
 
 
@@ -719,7 +728,8 @@ def main():
     ap.add_argument("--cpu-threads", type=int, default=0, help="host threads of the CPU legs (0: all)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--case", default="random_field", choices=["random_field", "hurricane", "fetch_limited"],
+    ap.add_argument("--case", default="random_field",
+                    choices=["random_field", "hurricane", "fetch_limited", "curvilinear"],
                     help="plain-path workload")
     ap.add_argument("--workload", default="random_field", choices=["random_field", "ensemble", "surrogate", "accuracy"])
     ap.add_argument("--acc-size", type=int, default=120, help="grid of the accuracy workloads")
@@ -768,6 +778,9 @@ def main():
                 "0.5 m/s current, 600 s forcing snapshots), plain path" % (args.size, args.size))
     elif args.case == "fetch_limited":
         desc = "fetch_limited %dx%d dx=5km, 1000 m, 10 m/s, plain path" % (args.size, args.size)
+    elif args.case == "curvilinear":
+        desc = ("random_field %dx%d on a skewed lon/lat grid (0.02 deg, about 2 km), curvilinear propagation, "
+                "plain path" % (args.size, args.size))
     else:
         desc = "random_field %dx%d dx=2km, plain path" % (args.size, args.size)
     # the CPU baseline runs the oracle on this same case before the GPU arm

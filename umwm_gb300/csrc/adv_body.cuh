@@ -82,8 +82,10 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
   constexpr bool ST = AdvSmem<G, H, CURV>::ST;
   // loads of E*: the read-only path, or in a persistent kernel (which wrote
   // E* in the same launch) loads cached in L2 only (ld.global.cg), which
-  // see the other CTAs' writes after the grid barrier.  E* is never written
-  // by this body, so its loads may be ordered freely against the e stores
+  // see the other CTAs' writes after the grid barrier (ordinary L1-cached
+  // loads measured the same there: 6.90 ms against 6.91 per propagation
+  // stage at 1000x1000).  E* is never written by this body, so its loads
+  // may be ordered freely against the e stores
   auto lde = [](const float* __restrict__ p) { return COH ? __ldcg(p) : __ldg(p); };
 
   const float dta = ctl->dta, dtr = ctl->dtr;
@@ -203,12 +205,15 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
   // half a row of e and E* at a time (fewer live registers); the rows at the
   // halves' edges and the neighbouring groups' edge rows are loaded again
   constexpr int NPART = UMWM_ADVECT_HALVES;  // parts of a row (2: halves)
-  constexpr bool HV = NPART > 1 && SW && ST && G == 2 && (H % (NPART > 1 ? NPART : 1) == 0);
+  // (two groups: plain grids, whose neighbour slots are swapped per group,
+  // and curvilinear grids, with the turned directions from shared memory;
+  // with four groups a lane's row already holds H = 9 directions)
+  constexpr bool HV = NPART > 1 && G == 2 && (H % (NPART > 1 ? NPART : 1) == 0);
   const size_t oPt = sidx(prm, 0, 0, jj);  // the point's row 0 (all groups)
   const int pprev = ((q + G - 1) % G) * H + H - 1, pnext = ((q + 1) % G) * H;
   // TMA: the own rows in shared memory.  jj (the ghost for padding lanes)
   // lies in this CTA's 64 points: a member's ghost is in its last tile
-  static_assert(!TMA || HV, "the TMA form is the two-group, plain-grid form with rows in halves");
+  static_assert(!TMA || (HV && SW && ST), "the TMA form is the two-group, plain-grid form with rows in halves");
   const int row = 2 * prm.P * 32;  // floats of one array (two blocks) in a buffer
   const int jl64 = jj - cta * PPC;
   const int sS = ((jl64 >> 5) * prm.P + q * H) * 32 + (jl64 & 31);  // the lane's row in a staged array
@@ -270,11 +275,12 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
     float DCA = 0.f, DCB = 0.f, DSA = 0.f, DSB = 0.f;
     float alc = 0.f, bec = 0.f, alp = 0.f, bep = 0.f, aln = 0.f, ben = 0.f, c0 = 0.f;
     if (prog) {
+      // the four face weights: per slot (SW), or east, west, north, south
       const float cgi = __ldg(T + tS + T_CG0 * 32);
-      DCA = 2.f * (cgi + __ldg(T + tCA + T_CG0 * 32)) * lCA;
-      DCB = 2.f * (cgi + __ldg(T + tCB + T_CG0 * 32)) * lCB;
-      DSA = 2.f * (cgi + __ldg(T + tSA + T_CG0 * 32)) * lSA;
-      DSB = 2.f * (cgi + __ldg(T + tSB + T_CG0 * 32)) * lSB;
+      DCA = 2.f * (cgi + __ldg(T + (SW ? tCA : tE) + T_CG0 * 32)) * (SW ? lCA : dye);
+      DCB = 2.f * (cgi + __ldg(T + (SW ? tCB : tW) + T_CG0 * 32)) * (SW ? lCB : dyw);
+      DSA = 2.f * (cgi + __ldg(T + (SW ? tSA : tN) + T_CG0 * 32)) * (SW ? lSA : dxn);
+      DSB = 2.f * (cgi + __ldg(T + (SW ? tSB : tSs) + T_CG0 * 32)) * (SW ? lSB : dxs);
     }
     if (refr) {
       const float gx = 0.5f * (__ldg(T + tE + T_CP0 * 32) - __ldg(T + tW + T_CP0 * 32));
@@ -312,13 +318,24 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
         for (int i = 0; i < HH; ++i) {
           const int k = k0 + i;
           const float e0 = es[i];
-          const float eca = stg[0][ST ? k : 0][threadIdx.x];
-          const float ecb = stg[1][ST ? k : 0][threadIdx.x];
-          const float esa = lde(ESo + oSA + k * 32), esb = lde(ESo + oSB + k * 32);
-          const float cp = prm.cthp[k], cm = prm.cthm[k], sp = prm.sthp[k], sm = prm.sthm[k];
-          float flux = DCA * (cp * e0 + cm * eca) - DCB * (cp * ecb + cm * e0) + DSA * (sp * e0 + sm * esa) -
-                       DSB * (sp * esb + sm * e0);
-          if (!zerocur) flux += F0 * e0 + kCA * eca + kCB * ecb + kSA * esa + kSB * esb;
+          float flux;
+          if (SW) {
+            const float eca = ST ? stg[0][ST ? k : 0][threadIdx.x] : lde(ESo + oCA + k * 32);
+            const float ecb = ST ? stg[1][ST ? k : 0][threadIdx.x] : lde(ESo + oCB + k * 32);
+            const float esa = lde(ESo + oSA + k * 32), esb = lde(ESo + oSB + k * 32);
+            const float cp = prm.cthp[k], cm = prm.cthm[k], sp = prm.sthp[k], sm = prm.sthm[k];
+            flux = DCA * (cp * e0 + cm * eca) - DCB * (cp * ecb + cm * e0) + DSA * (sp * e0 + sm * esa) -
+                   DSB * (sp * esb + sm * e0);
+            if (!zerocur) flux += F0 * e0 + kCA * eca + kCB * ecb + kSA * esa + kSB * esb;
+          } else {  // curvilinear: the directions turned by the grid's curvature
+            const float ee = lde(ESo + oE + k * 32), ew = lde(ESo + oW + k * 32);
+            const float en = lde(ESo + oN + k * 32), esn = lde(ESo + oSs + k * 32);
+            const float cc = ccs[CURV ? k : 0][threadIdx.x], sc = scs[CURV ? k : 0][threadIdx.x];
+            const float cp = fmaxf(cc, 0.f), cm = fminf(cc, 0.f), sp = fmaxf(sc, 0.f), sm = fminf(sc, 0.f);
+            flux = DCA * (cp * e0 + cm * ee) - DCB * (cp * ew + cm * e0) + DSA * (sp * e0 + sm * en) -
+                   DSB * (sp * esn + sm * e0);
+            if (!zerocur) flux += F0 * e0 + fedn * ee - fwup * ew + fndn * en - fsup * esn;
+          }
           ef[i] = ef[i] - dtaq * flux;
         }
         if (h == NPART - 1) stage(o + 1);  // the staged rows have been read

@@ -74,7 +74,7 @@ static void launch_adv(int minb, dim3 grid, const Params& prm, const Ptrs& P, cu
       return;
     }
   }
-  if constexpr (!CURV && G == 2 && H == 18) {
+  if constexpr (!CURV && G == 2 && H == 18 && UMWM_ADVECT_HALVES > 1) {  // the staged form takes rows in halves
     if (prm.adv_tma) {
       const size_t smem = tma_smem_bytes<18>(prm.P);
       static const cudaError_t attr =

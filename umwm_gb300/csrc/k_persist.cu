@@ -60,6 +60,27 @@ __device__ __forceinline__ bool grid_barrier(Global* g, unsigned expected, unsig
   return *ok_s != 0;
 }
 
+// The forcing interpolation of every member still inside the dtg, PREP_U
+// points per thread with their loads first (prep_points).  Measured on the
+// 1000x1000 random field (ms per substep, forcing / propagation / whole
+// substep): one point per thread 0.53 / 6.90 / 11.71; four points 0.20 /
+// 7.45 / 12.05 inlined and 0.20 / 7.51 / 12.40 as a separate function (the
+// larger register demand of the forcing stage costs the propagation more
+// than it saves).
+#ifndef UMWM_PERSIST_PREP_U
+#define UMWM_PERSIST_PREP_U 1
+#endif
+__device__ __forceinline__ void forcing_stage(const Params& prm, const Ptrs& P, int nb, int compute_rot) {
+  constexpr int U = UMWM_PERSIST_PREP_U;
+  for (int m = 0; m < prm.nmem; ++m) {
+    const Member& M = prm.mem[m];
+    Ctl* ctl = M.ctl;
+    if (ctl->done) continue;
+    for (int i = blockIdx.x * 128 + threadIdx.x; i < M.NM; i += U * nb * 128)
+      prep_points<U>(prm, P, M, ctl, i, nb * 128, compute_rot);
+  }
+}
+
 template <int G, int H, bool CURV>
 union PersistSmem {
   SrcSmem<G, H, false> phys;
@@ -69,7 +90,10 @@ union PersistSmem {
 };
 
 template <int G, int H, bool CURV>
-__global__ void __launch_bounds__(128, 4)
+#ifndef UMWM_PERSIST_MINB
+#define UMWM_PERSIST_MINB 4  // resident CTAs per SM (3, at 168 registers: 12.42 ms per substep against 11.71)
+#endif
+__global__ void __launch_bounds__(128, UMWM_PERSIST_MINB)
     k_persist(const Params prm, const Ptrs P, unsigned expected, unsigned long long limit_ns) {
   __shared__ PersistSmem<G, H, CURV> sm;
   __shared__ int ok_s;
@@ -91,13 +115,7 @@ __global__ void __launch_bounds__(128, 4)
   };
   const int budget = gl->budget;  // armed before the launch (k_loop_arm)
   for (int it = 0; it < budget; ++it) {
-    // forcing interpolation of every member still inside the dtg
-    for (int m = 0; m < prm.nmem; ++m) {
-      const Member& M = prm.mem[m];
-      Ctl* ctl = M.ctl;
-      if (ctl->done) continue;
-      for (int i = blockIdx.x * 128 + threadIdx.x; i < M.NM; i += nb * 128) prep_point(prm, P, M, ctl, i, compute_rot);
-    }
+    forcing_stage(prm, P, nb, compute_rot);
     if (!bar_s(0)) return;
     if (prm.ice_possible) {
       for (int j = blockIdx.x * 128 + threadIdx.x; j < prm.Ntot; j += nb * 128) sice_point(prm, P, j);
