@@ -815,7 +815,8 @@ def main():
         cfg = {k: int(U.stat("config:" + k)) for k in ("phys", "integ", "advect")}
         tune = {"mode": args.autotune, "substeps_measured": int(U.stat("autotune_substeps")),
                 "choice": {k: {"direction_groups": (v // 100) % 10, "ctas_per_sm": (v // 10) % 10 or "default",
-                               "prefetch_levels": v % 10, "own_rows_by_bulk_copy": bool(v // 1000)}
+                               "prefetch_levels": v % 10,
+                               "own_rows_by_bulk_copy": {0: False, 1: "E* and e", 2: "E*"}.get(v // 1000, v // 1000)}
                            for k, v in cfg.items()},
                 "median_ms": {k: {str(int(U.stat("tune_cfg:%s:%d" % (k, i)))): round(U.stat("tune_ms:%s:%d" % (k, i)), 4)
                                   for i in range(int(U.stat("tune_n:" + k)))} for k in cfg}}

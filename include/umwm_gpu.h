@@ -217,10 +217,11 @@ int umwm_gpu_get_screen(double* out, long n, long* rows);
  * "minb_advect" (resident CTAs per SM the kernel's register budget is sized
  * for; 0 or a budget without a compiled instance: the default) and
  * "pf_phys" / "pf_integ" / "pf_advect" (frequency levels each kernel
- * prefetches into L2 ahead), "advect_tma" / "phys_tma" (1: the
- * propagation / dts pre-pass of the two-group 36-direction mapping stage
- * each level's own rows in shared memory with bulk copies; results do not
- * change), "autotune" (0 off; 1: from the next substep
+ * prefetches into L2 ahead), "advect_tma" / "phys_tma" (the propagation /
+ * dts pre-pass of the two-group 36-direction mapping stage each level's own
+ * rows in shared memory with bulk copies: advect_tma 1 the E* and e rows,
+ * 2 the E* rows only; phys_tma 1 the e rows; results do not change),
+ * "autotune" (0 off; 1: from the next substep
  * on, time the register budgets and prefetch distances of the three
  * spectral kernels on the model's own substeps, round-robin, and keep the
  * fastest of each; results do not change; 2: also the direction mappings,

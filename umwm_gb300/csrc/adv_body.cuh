@@ -62,8 +62,9 @@ struct AdvSmem {
 // carries no counter).  COH: E* is read with coherent loads instead of the
 // read-only path, for a persistent kernel in which the same launch wrote it.
 // TMA: the own rows come from shared memory staged by bulk copies (OwnStage;
+// 1: the E* and e rows, 2: the E* rows only, e read as before;
 // the two-group, plain-grid mapping with rows in halves only).
-template <int G, int H, bool CURV, bool CNT, bool COH, bool TMA = false>
+template <int G, int H, bool CURV, bool CNT, bool COH, int TMA = 0>
 __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, int cta, AdvSmem<G, H, CURV>& sm,
                                             OwnStage own = OwnStage{nullptr, 0u}) {
   constexpr int PW = 32 / G;   // points per warp
@@ -227,14 +228,19 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
   const int sPt = ((jl64 >> 5) * prm.P) * 32 + (jl64 & 31);          // the point's row 0
   int occ = O;  // levels of which E* is staged: the CTA's largest cut-off
   const size_t src0 = sidx(prm, 0, 0, cta * PPC);
+  constexpr bool TEF = TMA == 1;     // e staged as well
+  constexpr int NA = TEF ? 2 : 1;    // arrays per buffer: E* (and e)
   auto issue = [&](int o) {  // one thread: level o's rows into buffer o & 1
     if (o >= O) return;
     const int b = o & 1;
     const uint32_t bar = own.mbar + 8u * b;
     const uint32_t bytes = (uint32_t)row * 4u;
-    adv_mbar_expect(bar, (o < occ ? 2u : 1u) * bytes);
-    adv_bulk_copy(adv_smem_u32(own.buf + (size_t)(2 * b + 1) * row), P.EF + src0 + (size_t)o * lstride, bytes, bar);
-    if (o < occ) adv_bulk_copy(adv_smem_u32(own.buf + (size_t)(2 * b) * row), P.ES + src0 + (size_t)o * lstride, bytes, bar);
+    // (a level above every cut-off of a CTA that stages E* only copies
+    // nothing: the arrival alone completes the phase)
+    adv_mbar_expect(bar, ((o < occ ? 1u : 0u) + (TEF ? 1u : 0u)) * bytes);
+    if (TEF)
+      adv_bulk_copy(adv_smem_u32(own.buf + (size_t)(NA * b + 1) * row), P.EF + src0 + (size_t)o * lstride, bytes, bar);
+    if (o < occ) adv_bulk_copy(adv_smem_u32(own.buf + (size_t)(NA * b) * row), P.ES + src0 + (size_t)o * lstride, bytes, bar);
   };
   if (TMA) {
     __shared__ int s_occ;
@@ -270,8 +276,8 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
         issue(o + 1);
       }
     }
-    const float* ownES = TMA ? own.buf + (size_t)(2 * (o & 1)) * row : nullptr;
-    const float* ownE = TMA ? own.buf + (size_t)(2 * (o & 1) + 1) * row : nullptr;
+    const float* ownES = TMA ? own.buf + (size_t)(NA * (o & 1)) * row : nullptr;
+    const float* ownE = TEF ? own.buf + (size_t)(NA * (o & 1) + 1) * row : nullptr;
     constexpr int HH = HV ? H / NPART : 1;
     const float* T = P.TAB + (size_t)o * tstride;
     const float* __restrict__ ESo = P.ES + (size_t)o * lstride;
@@ -317,7 +323,7 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
       const int k0 = h * HH;
       float ef[HH];
 #pragma unroll
-      for (int i = 0; i < HH; ++i) ef[i] = TMA ? ownE[sS + (k0 + i) * 32] : EFo[oS + (k0 + i) * 32];  // e below the cut-off, ef above
+      for (int i = 0; i < HH; ++i) ef[i] = TEF ? ownE[sS + (k0 + i) * 32] : EFo[oS + (k0 + i) * 32];  // e below the cut-off, ef above
       if (prog) {
         float es[HH];
 #pragma unroll

@@ -38,24 +38,25 @@ __global__ void __launch_bounds__(128, MINB) k_advect(const Params prm, const Pt
   advect_body<G, H, CURV, CNT, false>(prm, P, blockIdx.x, sm);
 }
 
-// k_advect_tma: the same body with each level's own E* and e rows staged in
-// shared memory by bulk copies (OwnStage), for the two-group plain-grid
-// mapping; 64.9 KB of shared memory per CTA, 3 CTAs per SM.
-template <int G, int H>
-__global__ void __launch_bounds__(128, 3) k_advect_tma(const Params prm, const Ptrs P) {
+// k_advect_tma: the same body with each level's own rows staged in shared
+// memory by bulk copies (OwnStage), for the two-group plain-grid mapping.
+// TM 1: the E* and e rows, 64.9 KB of shared memory per CTA, 3 CTAs per SM;
+// TM 2: the E* rows only, 47.1 KB, 4 CTAs per SM (128 registers).
+template <int G, int H, int TM>
+__global__ void __launch_bounds__(128, TM == 1 ? 3 : 4) k_advect_tma(const Params prm, const Ptrs P) {
   extern __shared__ __align__(128) unsigned char dsm[];
   __shared__ __align__(8) unsigned long long mbar[2];
   auto& sm = *reinterpret_cast<AdvSmem<G, H, false>*>(dsm);
   constexpr size_t off = (sizeof(AdvSmem<G, H, false>) + 127) & ~size_t(127);
   const OwnStage own{reinterpret_cast<float*>(dsm + off), adv_smem_u32(mbar)};
-  advect_body<G, H, false, false, false, true>(prm, P, blockIdx.x, sm, own);
+  advect_body<G, H, false, false, false, TM>(prm, P, blockIdx.x, sm, own);
 }
 
-// shared memory of k_advect_tma<2, H>: the AdvSmem and two buffers of two
-// arrays of the CTA's two blocks
+// shared memory of k_advect_tma<2, H, TM>: the AdvSmem and two buffers of
+// one or two arrays (TM 2 or 1) of the CTA's two blocks
 template <int H>
-constexpr size_t tma_smem_bytes(int pm) {
-  return ((sizeof(AdvSmem<2, H, false>) + 127) & ~size_t(127)) + (size_t)2 * 2 * 2 * pm * 32 * 4;
+constexpr size_t tma_smem_bytes(int pm, int tm) {
+  return ((sizeof(AdvSmem<2, H, false>) + 127) & ~size_t(127)) + (size_t)2 * (tm == 1 ? 2 : 1) * 2 * pm * 32 * 4;
 }
 
 // Launch with the register budget of `minb` resident CTAs per SM (tuned
@@ -75,12 +76,20 @@ static void launch_adv(int minb, dim3 grid, const Params& prm, const Ptrs& P, cu
     }
   }
   if constexpr (!CURV && G == 2 && H == 18 && UMWM_ADVECT_HALVES > 1) {  // the staged form takes rows in halves
-    if (prm.adv_tma) {
-      const size_t smem = tma_smem_bytes<18>(prm.P);
+    if (prm.adv_tma == 1) {
+      const size_t smem = tma_smem_bytes<18>(prm.P, 1);
       static const cudaError_t attr =
-          cudaFuncSetAttribute(k_advect_tma<2, 18>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+          cudaFuncSetAttribute(k_advect_tma<2, 18, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (attr == cudaSuccess) {
-        k_advect_tma<2, 18><<<grid, block, smem, st>>>(prm, P);
+        k_advect_tma<2, 18, 1><<<grid, block, smem, st>>>(prm, P);
+        return;
+      }
+    } else if (prm.adv_tma == 2) {
+      const size_t smem = tma_smem_bytes<18>(prm.P, 2);
+      static const cudaError_t attr =
+          cudaFuncSetAttribute(k_advect_tma<2, 18, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (attr == cudaSuccess) {
+        k_advect_tma<2, 18, 2><<<grid, block, smem, st>>>(prm, P);
         return;
       }
     }

@@ -110,7 +110,7 @@ struct MemberHost {
 // domain signature for the life of the process.
 struct TuneCand {
   int g4, minb, pf;  // quarter-turn groups, CTAs per SM (0: default instance), levels prefetched
-  int tma = 0;       // propagation only: own rows staged by bulk copies (k_advect_tma)
+  int tma = 0;       // own rows staged by bulk copies (propagation 1: E* and e, 2: E*; pre-pass 1: e)
 };
 struct KernelTune {
   std::vector<TuneCand> cands;
@@ -346,7 +346,10 @@ void tune_start(Model& M, int mode) {
       // the propagation (3 CTAs per SM) and the dts pre-pass (5) with their
       // own rows staged by bulk copies
       if (k == TK_ADVECT && d36 && !p.curvilinear && !g4)
-        for (int pf : pfs) K.cands.push_back({0, 3, pf, 1});
+        for (int pf : pfs) {
+          K.cands.push_back({0, 3, pf, 1});  // E* and e staged
+          K.cands.push_back({0, 4, pf, 2});  // E* staged
+        }
       if (k == TK_PHYS && d36 && !g4)
         for (int pf : {1, 2}) K.cands.push_back({0, 5, pf, 1});
     }
@@ -2217,7 +2220,9 @@ int umwm_gpu_set_option(const char* name, double value) {
     }
   }
   if (s == "advect_tma" || s == "phys_tma") {  // own rows staged by bulk copies (two groups, pm 36)
-    (s == "advect_tma" ? M->prm.adv_tma : M->prm.phys_tma) = value != 0 ? 1 : 0;
+    // advect_tma 1: E* and e rows, 2: E* rows only; phys_tma 1: e rows
+    (s == "advect_tma" ? M->prm.adv_tma : M->prm.phys_tma) =
+        s == "advect_tma" ? std::max(0, std::min(2, (int)value)) : (value != 0 ? 1 : 0);
     drop_graph(*M);
     return UMWM_OK;
   }
