@@ -62,6 +62,10 @@ __device__ __forceinline__ float sin_k(const Params& prm, const WindIn& w, float
 #define UMWM_INTEG_MINB 4  // resident CTAs per SM the register budget is sized for (two groups);
                            // with the lagged levels in shared memory: 122 registers, no spills
 #endif
+#ifndef UMWM_INTEG_PACKED
+#define UMWM_INTEG_PACKED 1  // the mss sums, the Sds factors and the integration step on direction
+                             // pairs in packed f32x2 arithmetic
+#endif
 #ifndef UMWM_INTEG_SMEM_LAGS
 #define UMWM_INTEG_SMEM_LAGS 1  // the integration keeps its two lagged levels in shared memory
                                 // (37 KB per CTA): 3.56 ms instead of 4.28 ms with them in registers
@@ -234,9 +238,26 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
       // the group's cos/sin 2th sign folded into the coefficients
       const float Bq = G == 4 ? c2s * B : B, Cq = G == 4 ? c2s * C : C;
       Cc.a = A; Cc.b = Bq; Cc.c = Cq;
+      // PKI: pairs of directions (k, k+1) in packed f32x2 arithmetic; an
+      // odd last direction takes the scalar form
+      constexpr bool PKI = UMWM_INTEG_PACKED;
+      constexpr int NPI = PKI ? H / 2 : 0;
       float s0 = 0.f, sc2 = 0.f, ss2 = 0.f;
+      if constexpr (PKI) {  // even and odd directions summed apart
+        float2 a0 = make_float2(0.f, 0.f), a1 = a0, a2 = a0;
 #pragma unroll
-      for (int k = 0; k < H; ++k) {
+        for (int n = 0; n < NPI; ++n) {
+          const float2 e = make_float2(ec[2 * n], ec[2 * n + 1]);
+          a0 = __fadd2_rn(a0, e);
+          a1 = __ffma2_rn(e, make_float2(prm.c2th[2 * n], prm.c2th[2 * n + 1]), a1);
+          a2 = __ffma2_rn(e, make_float2(prm.s2th[2 * n], prm.s2th[2 * n + 1]), a2);
+        }
+        s0 = a0.x + a0.y;
+        sc2 = a1.x + a1.y;
+        ss2 = a2.x + a2.y;
+      }
+#pragma unroll
+      for (int k = 2 * NPI; k < H; ++k) {
         s0 += ec[k];
         sc2 += ec[k] * prm.c2th[k];
         ss2 += ec[k] * prm.s2th[k];
@@ -256,8 +277,24 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
       // with the level's factors in the exponent: 2^(p log2 e + p log2 k4 + log2 sA)
       const float lsk = fmaf(prm.sds_power, lg2a(Lc.k4), lg2a(sA));
       if (INTEG || prog) {
+        if constexpr (PKI) {
+          const float2 a2 = make_float2(A, A), b2 = make_float2(Bq, Bq), c2 = make_float2(Cq, Cq);
+          const float2 mf = make_float2(prm.mss_fac, prm.mss_fac), one = make_float2(1.f, 1.f);
+          const float2 pw = make_float2(prm.sds_power, prm.sds_power), lk = make_float2(lsk, lsk);
 #pragma unroll
-        for (int k = 0; k < H; ++k) {
+          for (int n = 0; n < NPI; ++n) {
+            const int k = 2 * n;
+            const float2 chi = __ffma2_rn(c2, make_float2(prm.s2th[k], prm.s2th[k + 1]),
+                                          __ffma2_rn(b2, make_float2(prm.c2th[k], prm.c2th[k + 1]), a2));
+            const float2 t = __ffma2_rn(mf, chi, one);
+            const float2 x = __ffma2_rn(pw, make_float2(lg2a(ec[k]), lg2a(ec[k + 1])), lk);
+            const float2 r = __fmul2_rn(__fmul2_rn(t, t), make_float2(ex2a(x.x), ex2a(x.y)));
+            sc[k] = r.x;
+            sc[k + 1] = r.y;
+          }
+        }
+#pragma unroll
+        for (int k = 2 * NPI; k < H; ++k) {
           const float chi = A + Bq * prm.c2th[k] + Cq * prm.s2th[k];
           const float t = 1.f + prm.mss_fac * chi;
           sc[k] = (t * t) * ex2a(fmaf(prm.sds_power, lg2a(ec[k]), lsk));
@@ -312,8 +349,37 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
       float* EF = P.EF + sidx(prm, 0, q * H, jj) + (size_t)Lv * lstride;
       const size_t so = sidx(prm, 0, q * H, jj) + (size_t)Lv * lstride;  // saved source terms
       if (prog) {
+        constexpr bool PKI = UMWM_INTEG_PACKED && !SAVE;
+        constexpr int NPI = PKI ? H / 2 : 0;
+        if constexpr (PKI) {
+          // snl, the summed sinks and the exponential step of two directions
+          const float2 b1 = make_float2(L2.bf1r, L2.bf1r), b2 = make_float2(L2.bf2r, L2.bf2r);
+          const float2 nsf = make_float2(-prm.snl_fac, -prm.snl_fac), nct = make_float2(-L2.cothkd, -L2.cothkd);
+          const float2 nsk = make_float2(-sinkL, -sinkL), dl = make_float2(dtsl2, dtsl2), dd = make_float2(dts, dts);
+          const float2 half = make_float2(0.5f, 0.5f);
 #pragma unroll
-        for (int k = 0; k < H; ++k) {
+          for (int n = 0; n < NPI; ++n) {
+            const int k = 2 * n;
+            const float2 sn = make_float2(
+                sin_k(prm, wi, U, CW(k), ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0, L2.fkovg, false),
+                sin_k(prm, wi, U, CW(k + 1), ucg * prm.cth[k + 1], vcg * prm.sth[k + 1], L2.cp0, L2.fkovg, false));
+            const float2 pe2 = make_float2(LAG_E2(k), LAG_E2(k + 1)), ps2 = make_float2(LAG_S2(k), LAG_S2(k + 1));
+            const float2 pe1 = make_float2(LAG_E1(k), LAG_E1(k + 1)), ps1 = make_float2(LAG_S1(k), LAG_S1(k + 1));
+            float2 snl = __fmul2_rn(__fmul2_rn(b1, ps1), pe1);
+            snl = __ffma2_rn(__fmul2_rn(b2, make_float2(sc[k], sc[k + 1])), make_float2(ec[k], ec[k + 1]), snl);
+            snl = __ffma2_rn(__fmul2_rn(nsf, ps2), pe2, snl);
+            const float2 S = __fadd2_rn(__ffma2_rn(ps2, nct, sn), nsk);
+            const float2 x = __fmul2_rn(dl, S);
+            const float2 ef = __ffma2_rn(pe2, make_float2(ex2a(x.x), ex2a(x.y)), __fmul2_rn(dd, snl));
+            const float2 es = __fmul2_rn(half, __fadd2_rn(pe2, ef));
+            if (valid) {
+              ES[k * 32] = es.x;
+              ES[(k + 1) * 32] = es.y;
+            }
+          }
+        }
+#pragma unroll
+        for (int k = 2 * NPI; k < H; ++k) {
           const float s = sin_k(prm, wi, U, CW(k), ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0,
                                 L2.fkovg, false);
           const float e2k = LAG_E2(k), s2k = LAG_S2(k);
