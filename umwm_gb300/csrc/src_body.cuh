@@ -360,9 +360,9 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
 #pragma unroll
           for (int n = 0; n < NPI; ++n) {
             const int k = 2 * n;
-            const float2 sn = make_float2(
-                sin_k(prm, wi, U, CW(k), ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0, L2.fkovg, false),
-                sin_k(prm, wi, U, CW(k + 1), ucg * prm.cth[k + 1], vcg * prm.sth[k + 1], L2.cp0, L2.fkovg, false));
+            const float2 sn = sin_fold2(prm, wi.shelt, U, make_float2(CW(k), CW(k + 1)), ucg, vcg,
+                                        make_float2(prm.cth[k], prm.cth[k + 1]), make_float2(prm.sth[k], prm.sth[k + 1]),
+                                        L2.cp0, wi.c1 * L2.fkovg, false);
             const float2 pe2 = make_float2(LAG_E2(k), LAG_E2(k + 1)), ps2 = make_float2(LAG_S2(k), LAG_S2(k + 1));
             const float2 pe1 = make_float2(LAG_E1(k), LAG_E1(k + 1)), ps1 = make_float2(LAG_S1(k), LAG_S1(k + 1));
             float2 snl = __fmul2_rn(__fmul2_rn(b1, ps1), pe1);
