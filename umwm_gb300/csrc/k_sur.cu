@@ -13,9 +13,9 @@ namespace sur {
 
 namespace {
 
-constexpr int PITCHW = FPAD / 2 + 1;  // 32-bit words per staged row (odd: conflict-free columns)
 constexpr int UNR = 12;                // spectrum loads in flight per warp in the bin loops
-constexpr int TILE_SMEM = 32 * PITCHW * 4;
+constexpr int FLC = 8;                 // levels per chunk of k_features (one per warp)
+constexpr int FPITCHW = FLC * MAX_PM / 2 + 1;  // words per row of k_features' chunk tile (odd)
 
 struct PointInfo {
   int j, ok, s;
@@ -44,15 +44,19 @@ __device__ __forceinline__ float feature(float e) { return (logf(fmaxf(e, 0.f) +
 // error from feeding energy into bins the forcing does not reach.
 constexpr float GROWTH_SLACK = 0.02f;
 
-__device__ __forceinline__ __nv_bfloat16* row_h(uint32_t* tile, int r) {
-  return reinterpret_cast<__nv_bfloat16*>(tile + r * PITCHW);
-}
-
 }  // namespace
 
+// Input rows of 32 points per CTA (8 warps).  Warp 0 finds each row's
+// point, rotation and extra features.  The spectrum part goes level chunk
+// by level chunk (FLC levels, FLC * pm columns of every row): warp w takes
+// level w of the chunk, lane = row, and walks the directions (UNR loads in
+// flight), writing the rotated bf16 features into a shared-memory tile; the
+// tile's row segments then go out as 32-bit words, coalesced along each
+// row.  For the inference rows (pts == nullptr, row r = point r) a level's
+// row of 32 points is one 128-byte line per direction.
 __global__ void __launch_bounds__(256) k_features(const Params prm, const Ptrs P, const int* pts, int n,
                                                   __nv_bfloat16* X, float* ecopy, int* shift) {
-  extern __shared__ uint32_t tile[];
+  __shared__ uint32_t tile[32 * FPITCHW];
   __shared__ int s_j[32], s_ok[32], s_s[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int r0 = blockIdx.x * 32;
@@ -83,37 +87,43 @@ __global__ void __launch_bounds__(256) k_features(const Params prm, const Ptrs P
       ex[7] = P.rhorat[ja] * 800.f;
       ex[8] = P.fice[ja];
     }
-    __nv_bfloat16* h = row_h(tile, lane);
-    for (int c = F0; c < FPAD; ++c) h[c] = __float2bfloat16_rn(c - F0 < NEXTRA ? ex[c - F0] : 0.f);
+    if (r < n) {  // the extra features and the padding, straight to the row
+      for (int c = F0; c < FPAD; ++c)
+        X[(size_t)r * FPAD + c] = __float2bfloat16_rn(c - F0 < NEXTRA ? ex[c - F0] : 0.f);
+    }
   }
   __syncthreads();
   const int j = s_j[lane], ok = s_ok[lane], s = s_s[lane];
-  __nv_bfloat16* h = row_h(tile, lane);
-  // UNR independent loads in flight per warp before any is used
-  for (int b0 = warp; b0 < F0; b0 += 8 * UNR) {
-    float ev[UNR];
-#pragma unroll
-    for (int u = 0; u < UNR; ++u) {
-      const int b = b0 + 8 * u;
-      const int o = b / NP, p = b - o * NP;
-      ev[u] = (ok && b < F0) ? __ldg(P.E + sidx(prm, o, p, j)) : 0.f;
-    }
-#pragma unroll
-    for (int u = 0; u < UNR; ++u) {
-      const int b = b0 + 8 * u;
-      if (b >= F0) break;
-      const int o = b / NP, p = b - o * NP;
-      int pr = p - s;
-      if (pr < 0) pr += NP;
-      h[o * NP + pr] = __float2bfloat16_rn(ok ? feature(ev[u]) : 0.f);
-      if (ecopy && r0 + lane < n) ecopy[(size_t)(r0 + lane) * F0 + o * NP + pr] = ev[u];
-    }
-  }
-  __syncthreads();
+  __nv_bfloat16* h = reinterpret_cast<__nv_bfloat16*>(tile + lane * FPITCHW);
   uint32_t* X32 = reinterpret_cast<uint32_t*>(X);
-  for (int rr = warp; rr < 32; rr += 8) {
-    if (r0 + rr >= n) break;
-    for (int k = lane; k < FPAD / 2; k += 32) X32[(size_t)(r0 + rr) * (FPAD / 2) + k] = tile[rr * PITCHW + k];
+  for (int c0 = 0; c0 < prm.O; c0 += FLC) {
+    const int nl = min(FLC, prm.O - c0);  // levels of this chunk
+    const int o = c0 + warp;
+    if (warp < nl) {
+      const float* Er = ok ? P.E + sidx(prm, o, 0, j) : nullptr;  // direction p at Er[p * 32]
+      int pr = s == 0 ? 0 : NP - s;                                  // rotated column of p = 0
+      for (int p0 = 0; p0 < NP; p0 += UNR) {
+        float ev[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) ev[u] = (ok && p0 + u < NP) ? __ldg(Er + (p0 + u) * 32) : 0.f;
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+          if (p0 + u >= NP) break;
+          h[warp * NP + pr] = __float2bfloat16_rn(ok ? feature(ev[u]) : 0.f);
+          if (ecopy && r0 + lane < n) ecopy[(size_t)(r0 + lane) * F0 + o * NP + pr] = ev[u];
+          pr = pr + 1 == NP ? 0 : pr + 1;
+        }
+      }
+    }
+    __syncthreads();
+    // rows r0..r0+31, columns c0 * NP .. (c0 + nl) * NP, as words
+    const int nw = nl * NP / 2;
+    for (int rr = warp; rr < 32; rr += 8) {
+      if (r0 + rr >= n) break;
+      uint32_t* dst = X32 + ((size_t)(r0 + rr) * FPAD + (size_t)c0 * NP) / 2;
+      for (int k = lane; k < nw; k += 32) dst[k] = tile[rr * FPITCHW + k];
+    }
+    __syncthreads();
   }
 }
 
@@ -374,11 +384,9 @@ static int grid_for(size_t n, int block) {
 
 cudaError_t launch_features(const Params& prm, const Ptrs& P, const int* pts, int n, __nv_bfloat16* X,
                             float* ecopy, int* shift, cudaStream_t st) {
-  static cudaError_t attr = cudaFuncSetAttribute(k_features, cudaFuncAttributeMaxDynamicSharedMemorySize, TILE_SMEM);
-  if (attr != cudaSuccess) return attr;
-  if (prm.O * prm.P + NEXTRA > FPAD) return cudaErrorInvalidValue;
+  if (prm.O * prm.P + NEXTRA > FPAD || prm.P % 2) return cudaErrorInvalidValue;
   if (n <= 0) return cudaSuccess;
-  k_features<<<(n + 31) / 32, 256, TILE_SMEM, st>>>(prm, P, pts, n, X, ecopy, shift);
+  k_features<<<(n + 31) / 32, 256, 0, st>>>(prm, P, pts, n, X, ecopy, shift);
   return cudaGetLastError();
 }
 
