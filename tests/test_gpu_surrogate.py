@@ -23,8 +23,13 @@ def mo():
     return mlp_oracle
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (300, 256, 192), (1000, 1344, 512), (4096, 512, 1344)])
+@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (300, 256, 192), (1000, 1344, 512), (4096, 512, 1344),
+                                   (20480, 256, 128), (3328, 1344, 512), (40000, 512, 1344)])
 def test_gemm_bf16(lib_built, mo, M, N, K):
+    """Both tile widths: 128-wide tiles for launches with fewer 256-wide
+    tiles than SMs (the first four shapes), 256-wide ones otherwise (an
+    N tail of 64 columns in 3328 x 1344; several tiles per CTA and both
+    TMEM accumulators in turn in 40000 x 512)."""
     U = lib_built
     rng = np.random.default_rng(M + N + K)
     A = rng.standard_normal((M, K)).astype(np.float32)

@@ -2,6 +2,7 @@
 // host launcher.  See tc_gemm.cuh for the pipeline.
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <mutex>
 
@@ -77,24 +78,30 @@ __device__ __forceinline__ void epilogue(const EpiArgs& ep, int row, int col, co
   }
 }
 
-template <int EPI>
-__global__ void __launch_bounds__(THREADS, 2)
+template <int EPI, int BN_>
+__global__ void __launch_bounds__(THREADS, 1)
     k_gemm(const __grid_constant__ CUtensorMap ta, const __grid_constant__ CUtensorMap tb, int M, int N, int K,
            EpiArgs ep, int* err) {
+  using C = Cfg<BN_>;
+  constexpr int BN = C::BN, STAGES = C::STAGES, STAGE_BYTES = C::STAGE_BYTES, TMEM_COLS = C::TMEM_COLS;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], accum_bar;
+  __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], acc_full[2], acc_empty[2], mma_done;
   __shared__ uint32_t tmem_slot;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t base = (smem_u32(smem_raw) + 1023u) & ~1023u;
-  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
   const int KB = K / BK;
+  const int ntn = (N + BN - 1) / BN, ntiles = ntn * ((M + BM - 1) / BM);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(smem_u32(&full_bar[s]), 1);
       mbar_init(smem_u32(&empty_bar[s]), 1);
     }
-    mbar_init(smem_u32(&accum_bar), 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&acc_full[b]), 1);
+      mbar_init(smem_u32(&acc_empty[b]), 32 * EPI_WARPS);
+    }
+    mbar_init(smem_u32(&mma_done), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) tmem_alloc(smem_u32(&tmem_slot), TMEM_COLS);
@@ -106,57 +113,79 @@ __global__ void __launch_bounds__(THREADS, 2)
 
   if (warp == 0) {
     if (lane == 0) {
-      // producer: TMA loads of A and B k-blocks into the stage ring
-      int issued = 0;
-      for (int kb = 0; kb < KB; ++kb) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (kb / STAGES) & 1;
-        if (kb >= STAGES && !mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1)) {
-          ok = false;
-          break;
+      // producer: TMA loads of A and B k-blocks into the stage ring, tile after tile
+      int it = 0;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        const int m0 = (t / ntn) * BM, n0 = (t % ntn) * BN;
+        for (int kb = 0; kb < KB; ++kb, ++it) {
+          const int s = it % STAGES;
+          if (it >= STAGES && !mbar_wait(smem_u32(&empty_bar[s]), ((it / STAGES) & 1) ^ 1)) {
+            ok = false;
+            break;
+          }
+          const uint32_t a = base + s * STAGE_BYTES, b = a + A_TILE_BYTES;
+          mbar_expect_tx(smem_u32(&full_bar[s]), STAGE_BYTES);
+          tma_load_2d(a, &ta, kb * BK, m0, smem_u32(&full_bar[s]));
+          tma_load_2d(b, &tb, kb * BK, n0, smem_u32(&full_bar[s]));
         }
-        const uint32_t a = base + s * STAGE_BYTES, b = a + A_TILE_BYTES;
-        mbar_expect_tx(smem_u32(&full_bar[s]), STAGE_BYTES);
-        tma_load_2d(a, &ta, kb * BK, m0, smem_u32(&full_bar[s]));
-        tma_load_2d(b, &tb, kb * BK, n0, smem_u32(&full_bar[s]));
-        issued = kb + 1;
       }
       // drain: the last load of each stage has landed (bounded)
-      for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; ++kb)
-        if (!mbar_wait(smem_u32(&full_bar[kb % STAGES]), (kb / STAGES) & 1)) ok = false;
+      for (int i = (it > STAGES ? it - STAGES : 0); i < it; ++i)
+        if (!mbar_wait(smem_u32(&full_bar[i % STAGES]), (i / STAGES) & 1)) ok = false;
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      // MMA issuer: 4 x (M=128, N=128, K=16) per k-block, accumulate in TMEM
+      // MMA issuer: 4 x (M=128, N=BN, K=16) per k-block into accumulator tl & 1
       const uint32_t idesc = idesc_bf16(BM, BN);
-      for (int kb = 0; kb < KB; ++kb) {
-        const int s = kb % STAGES;
-        if (!mbar_wait(smem_u32(&full_bar[s]), (kb / STAGES) & 1)) {
+      int it = 0, tl = 0;
+      for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++tl) {
+        const int buf = tl & 1, use = tl >> 1;
+        // the epilogue has read this accumulator's previous tile
+        if (use > 0 && !mbar_wait(smem_u32(&acc_empty[buf]), (use - 1) & 1)) {
           ok = false;
           break;
         }
         tc_fence_after();
-        const uint32_t a = base + s * STAGE_BYTES, b = a + A_TILE_BYTES;
+        const uint32_t d = tmem + (uint32_t)(buf * BN);
+        for (int kb = 0; kb < KB; ++kb, ++it) {
+          const int s = it % STAGES;
+          if (!mbar_wait(smem_u32(&full_bar[s]), (it / STAGES) & 1)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a = base + s * STAGE_BYTES, b = a + A_TILE_BYTES;
 #pragma unroll
-        for (int k = 0; k < BK / 16; ++k)
-          umma_bf16(tmem, sw128_desc(a + k * 32), sw128_desc(b + k * 32), idesc, (kb | k) ? 1u : 0u);
-        umma_commit(smem_u32(&empty_bar[s]));
+          for (int k = 0; k < BK / 16; ++k)
+            umma_bf16(d, sw128_desc(a + k * 32), sw128_desc(b + k * 32), idesc, (kb | k) ? 1u : 0u);
+          umma_commit(smem_u32(&empty_bar[s]));
+        }
+        if (ok) umma_commit(smem_u32(&acc_full[buf]));  // arrives once the tile's MMAs have completed
       }
-      umma_commit(smem_u32(&accum_bar));  // arrives once every issued MMA has completed
+      // every MMA issued has completed before the TMEM is freed (bounded)
+      umma_commit(smem_u32(&mma_done));
+      if (!mbar_wait(smem_u32(&mma_done), 0)) ok = false;
     }
   } else {
-    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31, one C row per thread
-    ok = mbar_wait(smem_u32(&accum_bar), 0);
-    ok = __all_sync(0xffffffffu, ok);
-    tc_fence_after();
-    if (ok) {
-      const int q = warp & 3;
+    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 (one C row per
+    // thread) and half the accumulator's columns
+    const int q = warp & 3, h = (warp - 2) >> 2;
+    int tl = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl) {
+      const int buf = tl & 1, use = tl >> 1;
+      ok = mbar_wait(smem_u32(&acc_full[buf]), use & 1);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) break;
+      tc_fence_after();
+      const int m0 = (t / ntn) * BM, n0 = (t % ntn) * BN;
       const int row = m0 + q * 32 + lane;
-      for (int c = 0; c < BN; c += 32) {
+      for (int c = h * (BN / 2); c < (h + 1) * (BN / 2); c += 32) {
         float v[32];
-        tmem_ld32(tmem + (static_cast<uint32_t>(q * 32) << 16) + c, v);
+        tmem_ld32(tmem + (static_cast<uint32_t>(q * 32) << 16) + (uint32_t)(buf * BN + c), v);
         if (row < M && n0 + c < N) epilogue<EPI>(ep, row, n0 + c, v);
       }
+      tc_fence_before();
+      mbar_arrive(smem_u32(&acc_empty[buf]));
     }
   }
   if (!ok) atomicExch(err, 1);
@@ -202,22 +231,40 @@ cudaError_t make_map(CUtensorMap* m, const void* ptr, uint64_t rows, uint64_t co
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-template <int EPI>
-cudaError_t launch(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K, const EpiArgs& ep, int* err,
-                   cudaStream_t st) {
+template <int EPI, int BN>
+cudaError_t launch_bn(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K, const EpiArgs& ep,
+                      int* err, int nsm, cudaStream_t st) {
   static std::once_flag once;
   static cudaError_t attr = cudaSuccess;
   std::call_once(once, [] {
-    attr = cudaFuncSetAttribute(k_gemm<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    attr = cudaFuncSetAttribute(k_gemm<EPI, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<BN>::SMEM_BYTES);
   });
   if (attr != cudaSuccess) return attr;
   CUtensorMap ta, tb;
   cudaError_t e = make_map(&ta, A, M, K, BM);
   if (e == cudaSuccess) e = make_map(&tb, B, N, K, BN);
   if (e != cudaSuccess) return e;
-  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-  k_gemm<EPI><<<grid, THREADS, SMEM_BYTES, st>>>(ta, tb, M, N, K, ep, err);
+  const long tiles = (long)((N + BN - 1) / BN) * ((M + BM - 1) / BM);
+  const int grid = (int)std::min<long>(tiles, nsm);  // persistent: one CTA per SM
+  k_gemm<EPI, BN><<<grid, THREADS, Cfg<BN>::SMEM_BYTES, st>>>(ta, tb, M, N, K, ep, err);
   return cudaGetLastError();
+}
+
+// 256-wide tiles when they fill the SMs, else 128-wide ones
+template <int EPI>
+cudaError_t launch(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int N, int K, const EpiArgs& ep, int* err,
+                   cudaStream_t st) {
+  static int nsm = 0;
+  if (nsm == 0) {
+    int dev = 0, n = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    nsm = n;
+  }
+  const long tiles256 = (long)((N + 255) / 256) * ((M + BM - 1) / BM);
+  return tiles256 >= nsm ? launch_bn<EPI, 256>(A, B, M, N, K, ep, err, nsm, st)
+                         : launch_bn<EPI, 128>(A, B, M, N, K, ep, err, nsm, st);
 }
 
 }  // namespace
@@ -228,7 +275,7 @@ cudaError_t gemm_bf16(const __nv_bfloat16* A, const __nv_bfloat16* B, int M, int
                       const tc::EpiArgs& ep, int* err, cudaStream_t st) {
   using namespace tc;
   if (M <= 0 || N <= 0 || K <= 0 || K % BK || N % 32 || ep.ldo % 8 || (ep.ldz && ep.ldz % 8) ||
-      (reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(B) & 15) || M > 65535 * BM)
+      (reinterpret_cast<uintptr_t>(A) & 15) || (reinterpret_cast<uintptr_t>(B) & 15))
     return cudaErrorInvalidValue;
   switch (epi) {
     case EPI_F32: return launch<EPI_F32>(A, B, M, N, K, ep, err, st);

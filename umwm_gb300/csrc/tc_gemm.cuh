@@ -3,15 +3,19 @@
 //
 //   C[M x N] = A[M x K] * B[N x K]^T      (A, B bf16, K contiguous; fp32 accumulate)
 //
-// One CTA computes a 128 x 128 tile of C.  Warp 0 (one thread) streams
-// 128 x 64 tiles of A and B into shared memory with TMA (128-byte swizzle)
-// through a 3-stage mbarrier ring; warp 1 owns the TMEM accumulator (128
-// columns) and one of its threads issues tcgen05.mma (M=128, N=128, K=16,
-// 4 per 64-wide k-block), committing each stage back to the producer;
-// warps 2-5 read the accumulator with tcgen05.ld (one row per thread) and run
-// the epilogue.  Every mbarrier wait is bounded in time: on timeout the
-// kernel records an error in *err, drains its own TMA copies (bounded),
-// frees its TMEM and returns.
+// Persistent: one CTA per SM walks the 128 x 256 (or 128 x 128) output tiles (tile t =
+// blockIdx.x + i * gridDim.x, the tiles of one 128-row block next to each
+// other, so the block's next tile finds A in L2).  Warp 0 (one thread)
+// streams 128 x 64 tiles of A and 256 x 64 tiles of B into shared memory
+// with TMA (128-byte swizzle) through a 4-stage mbarrier ring; warp 1 owns
+// the TMEM (two 256-column fp32 accumulators) and one of its threads issues
+// tcgen05.mma (M=128, N=256, K=16, 4 per 64-wide k-block),
+// committing each stage back to the producer and each finished tile to the
+// epilogue; warps 2-9 read an accumulator with tcgen05.ld (one row per
+// thread, half the columns per warp) and run the epilogue while the next
+// tile accumulates in the other buffer.  Every mbarrier wait is bounded in
+// time: on timeout the kernel records an error in *err, drains its own TMA
+// copies and MMAs (bounded), frees its TMEM and returns.
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -22,13 +26,22 @@
 namespace umwm {
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 3;
-constexpr int A_TILE_BYTES = BM * BK * 2;                   // 16 KB
-constexpr int B_TILE_BYTES = BN * BK * 2;                   // 16 KB
-constexpr int STAGE_BYTES = A_TILE_BYTES + B_TILE_BYTES;    // 32 KB
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;     // + alignment slack
-constexpr int THREADS = 192;
-constexpr int TMEM_COLS = 128;
+constexpr int BM = 128, BK = 64;
+constexpr int A_TILE_BYTES = BM * BK * 2;  // 16 KB
+constexpr int EPI_WARPS = 8;
+constexpr int THREADS = 32 * (2 + EPI_WARPS);
+
+// Tile width BN: 256 (4 stages of 48 KB), or 128 (6 stages of 32 KB) for
+// launches with fewer 256-wide tiles than SMs (the small training GEMMs).
+template <int BN_>
+struct Cfg {
+  static constexpr int BN = BN_;
+  static constexpr int STAGES = BN_ == 256 ? 4 : 6;
+  static constexpr int B_TILE_BYTES = BN_ * BK * 2;
+  static constexpr int STAGE_BYTES = A_TILE_BYTES + B_TILE_BYTES;
+  static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;  // + alignment slack
+  static constexpr int TMEM_COLS = 2 * BN_;                       // two accumulators
+};
 constexpr long long WAIT_CYCLES = 4000000000LL;  // about 2 s at 2 GHz
 
 // Epilogue modes.
@@ -61,6 +74,10 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
