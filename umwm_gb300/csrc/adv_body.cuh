@@ -189,7 +189,7 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
     if (o < O && lane == 0) {
       if (o < ocw) bulk_prefetch(P.ES + blk + (size_t)o * lstride, (unsigned)(prm.P * 128));
       bulk_prefetch(P.EF + blk + (size_t)o * lstride, (unsigned)(prm.P * 128));
-      if (UMWM_PREFETCH_TAB) bulk_prefetch(P.TAB + tblk + (size_t)o * tstride, (unsigned)(T_COUNT * 128));
+      if (UMWM_PREFETCH_TAB) bulk_prefetch(P.TAB + tblk + (size_t)o * tstride, (unsigned)(T_ADV_ROWS * 128));
     }
   };
   const int PFD = prm.pf_adv;  // levels prefetched ahead (a tunable)

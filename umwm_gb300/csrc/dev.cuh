@@ -23,16 +23,18 @@ constexpr int MAX_OM = 64;
 constexpr int MAX_PM = 72;
 constexpr int MAX_LM = 100;
 
-// per-(o,i) table rows (stored per frequency o, then table, then point)
+// per-(o,i) table rows (stored per frequency o, then table, then point);
+// the rows the propagation reads come first (T_ADV_ROWS of them), so that
+// it prefetches only those
 enum TableRow {
   T_K = 0,      // wavenumber k                       umwm_init.F90:1473
   T_CP0,        // phase speed cp0 (ghost = min)      :1493, :1653-1656
   T_CG0,        // group velocity cg0 (ghost = min)   :1494, :1653-1656
   T_LOGL2Z,     // log(l2/z), capped                  :1530-1533
   T_FKOVG,      // f k / g                            :1507
+  T_KDK,        // k dk                               :1505
   T_K4,         // k^4                                :1503
   T_K3DK,       // k^3 dk                             :1506
-  T_KDK,        // k dk                               :1505
   T_COTHKD,     // coth(0.2 kd)                       :1508
   T_SBF,        // bottom friction+percolation        :1510-1511
   T_SDV,        // viscous dissipation                :1512
@@ -40,6 +42,7 @@ enum TableRow {
   T_BF2R,       // Snl weight to o+2                  :1524
   T_COUNT
 };
+constexpr int T_ADV_ROWS = T_KDK + 1;  // rows 0 .. T_KDK: all the propagation and stress read
 
 constexpr int TILE = 64;  // wet points of a tile (a member's points start on a tile boundary)
 

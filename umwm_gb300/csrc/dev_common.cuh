@@ -35,7 +35,7 @@ __device__ __forceinline__ float shelter_coare35(float w) {
 // Per-point inputs of the wind-input source term, sin_d12
 // (umwm_source_functions.F90:16-82).
 struct WindIn {
-  float wspd, uc, vc, ustar25, shelt_sf, shelt, c1;
+  float wspd, uc, vc, ustar25, shelt, c1;
   int oc;  // 1-based cut-off index; 0-based level o is prognostic when o < oc
 };
 
@@ -47,7 +47,6 @@ __device__ __forceinline__ WindIn load_wind(const Params& prm, const Ptrs& P, in
   w.vc = P.vc[ja];
   w.ustar25 = 2.5f * ustar;
   w.shelt = P.shelt[jj];
-  w.shelt_sf = w.shelt / prm.sin_fac;
   // (1 - fice) * twopi * rhorat
   w.c1 = ((1.f - P.fice[ja]) * (2.f * 3.14159274f)) * P.rhorat[ja];
   w.oc = P.oc[jj];
@@ -56,19 +55,6 @@ __device__ __forceinline__ WindIn load_wind(const Params& prm, const Ptrs& P, in
 
 // all-point index of a wet (or ghost) point of member M
 __device__ __forceinline__ int apt(const Member& M, int j) { return M.nmoff + (j - M.off); }
-
-// Sin at (o, p) given cw = cos(wdir - th(p)) and the level tables.
-__device__ __forceinline__ float sin_bin(const Params& prm, const WindIn& w, float cw, float cth, float sth,
-                                         float logl2z, float cp0, float fkovg, bool tail) {
-  float s = (w.wspd + w.ustar25 * logl2z) * cw - cp0 - w.uc * cth - w.vc * sth;
-  s = (prm.sin_fac * fabsf(s)) * s;
-  if (s > 0.f) s = s * w.shelt_sf;
-  if (s < 0.f) s = s * prm.fieldscale1;
-  if (s < 0.f && cw > 0.f) s = s * prm.fieldscale2;
-  s = (w.c1 * s) * fkovg;
-  if (tail) s = fmaxf(s, 0.f);
-  return s;
-}
 
 // Sin of one bin from x = U cos(wdir - th) - cp0 - uc cos th - vc sin th,
 // umwm_source_functions.F90:39-80, with its factors folded: the reference

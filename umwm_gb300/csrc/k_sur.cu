@@ -205,9 +205,11 @@ __global__ void __launch_bounds__(256) k_apply(const Params prm, const Ptrs P, c
     int pr = p - s;
     if (pr < 0) pr += NP;
     const float y = __uint_as_float((uint32_t)yb[lane * YP + pr] << 16);
-    sp = fmaxf(sin_bin(prm, wi, cwt[p * 32 + lane], prm.cth[p], prm.sth[p], logl2z, cp0, fkovg, tail), 0.f);
+    const float cw = cwt[p * 32 + lane];
+    const float x = (wi.wspd + wi.ustar25 * logl2z) * cw - cp0 - wi.uc * prm.cth[p] - wi.vc * prm.sth[p];
+    sp = fmaxf(sin_fold(prm, wi.shelt, x, cw, wi.c1 * fkovg, tail), 0.f);
     const float d = fminf(TS * y, dts * sp + GROWTH_SLACK);
-    return fmaxf((fmaxf(e, 0.f) + EPS) * expf(d) - EPS, 0.f);
+    return fmaxf((fmaxf(e, 0.f) + EPS) * ex2_approx(d * 1.44269504f) - EPS, 0.f);  // e^d through the SFU
   };
   float m0 = 0.f, m1 = 0.f, w0 = 0.f, w1 = 0.f;  // energy, and energy where the wind feeds (weight Sin)
   for (int o = warp; o < O; o += 8) {

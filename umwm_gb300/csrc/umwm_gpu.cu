@@ -442,8 +442,11 @@ int upload_tables(Model& M, const MemberHost& mh) {
   const Params& prm = M.prm;
   const int O = prm.O;
   const HostModel& H = mh.H;
-  const std::vector<float>* src[T_COUNT] = {&H.k, &H.cp0, &H.cg0, &H.logl2overz, &H.fkovg, &H.k4, &H.k3dk,
-                                            &H.kdk, &H.cothkd, &H.sbf, &H.sdv, &H.bf1r, &H.bf2r};
+  const std::vector<float>* src[T_COUNT] = {};
+  src[T_K] = &H.k, src[T_CP0] = &H.cp0, src[T_CG0] = &H.cg0, src[T_LOGL2Z] = &H.logl2overz;
+  src[T_FKOVG] = &H.fkovg, src[T_KDK] = &H.kdk, src[T_K4] = &H.k4, src[T_K3DK] = &H.k3dk;
+  src[T_COTHKD] = &H.cothkd, src[T_SBF] = &H.sbf, src[T_SDV] = &H.sdv, src[T_BF1R] = &H.bf1r;
+  src[T_BF2R] = &H.bf2r;
   const size_t per_o = (size_t)mh.padded * T_COUNT;  // floats of one level of this member
   std::vector<float> T(per_o);
   for (int o = 1; o <= O; ++o) {
