@@ -136,10 +136,11 @@ __global__ void __launch_bounds__(THREADS, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       // MMA issuer: 4 x (M=128, N=BN, K=16) per k-block into accumulator tl & 1
-      const uint32_t idesc = idesc_bf16(BM, BN);
+      // (N = the valid columns, a multiple of 32, for the last column tile)
       int it = 0, tl = 0;
       for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++tl) {
         const int buf = tl & 1, use = tl >> 1;
+        const uint32_t idesc = idesc_bf16(BM, min(BN, N - (t % ntn) * BN));
         // the epilogue has read this accumulator's previous tile
         if (use > 0 && !mbar_wait(smem_u32(&acc_empty[buf]), (use - 1) & 1)) {
           ok = false;
