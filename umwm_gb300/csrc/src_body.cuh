@@ -402,8 +402,38 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
         // 2^((log2 num - 2 log2 t) / p + lt0) with the level's part lt0
         const float sAc = prm.twopisds_fac * prm.f[Lv];
         const float lt0 = -fmaf(prm.inv_sds_power, lg2a(sAc * L2.cothkd), lg2a(L2.k4));
+        constexpr bool PKT = UMWM_INTEG_PACKED && !SAVE;
+        constexpr int NPT = PKT ? H / 2 : 0;
+        if constexpr (PKT) {  // two directions at a time, packed f32x2
+          const float2 nk = make_float2(sice - sdt - L2.sdv, sice - sdt - L2.sdv);
+          const float2 ca = make_float2(C2.a, C2.a), cb = make_float2(C2.b, C2.b), cc = make_float2(C2.c, C2.c);
+          const float2 mf = make_float2(prm.mss_fac, prm.mss_fac), one = make_float2(1.f, 1.f);
+          const float2 ip = make_float2(prm.inv_sds_power, prm.inv_sds_power), l0 = make_float2(lt0, lt0);
+          const float2 m2 = make_float2(-2.f, -2.f), half = make_float2(0.5f, 0.5f);
 #pragma unroll
-        for (int k = 0; k < H; ++k) {
+          for (int n = 0; n < NPT; ++n) {
+            const int k = 2 * n;
+            const float2 sn = sin_fold2(prm, wi.shelt, U, make_float2(CW(k), CW(k + 1)), ucg, vcg,
+                                        make_float2(prm.cth[k], prm.cth[k + 1]), make_float2(prm.sth[k], prm.sth[k + 1]),
+                                        L2.cp0, wi.c1 * L2.fkovg, true);
+            const float2 num = __fadd2_rn(sn, nk);
+            const float2 chi = __ffma2_rn(cc, make_float2(prm.s2th[k], prm.s2th[k + 1]),
+                                          __ffma2_rn(cb, make_float2(prm.c2th[k], prm.c2th[k + 1]), ca));
+            const float2 t = __ffma2_rn(mf, chi, one);
+            const float2 x = __ffma2_rn(ip, __ffma2_rn(m2, make_float2(lg2a(t.x), lg2a(t.y)),
+                                                       make_float2(lg2a(num.x), lg2a(num.y))), l0);
+            const float2 ef = make_float2(num.x >= 0.f ? ex2a(x.x) : 0.f, num.y >= 0.f ? ex2a(x.y) : 0.f);
+            const float2 es = __fmul2_rn(half, __fadd2_rn(make_float2(LAG_E2(k), LAG_E2(k + 1)), ef));
+            if (valid) {
+              ES[k * 32] = es.x;
+              ES[(k + 1) * 32] = es.y;
+              EF[k * 32] = ef.x;
+              EF[(k + 1) * 32] = ef.y;
+            }
+          }
+        }
+#pragma unroll
+        for (int k = 2 * NPT; k < H; ++k) {
           const float s = sin_k(prm, wi, U, CW(k), ucg * prm.cth[k], vcg * prm.sth[k], L2.cp0,
                                 L2.fkovg, true);
           const float num = s - sdt - L2.sdv + sice;
