@@ -315,20 +315,13 @@ __device__ __forceinline__ void source_body(const Params& prm, const Ptrs& P, in
           const float* CP = P.TAB + (size_t)o * tstride + T_CP0 * 32;
           const float dcx = __ldg(CP + tidx(prm, 0, 0, nie)) - __ldg(CP + tidx(prm, 0, 0, niw));
           const float dcy = __ldg(CP + tidx(prm, 0, 0, nin)) - __ldg(CP + tidx(prm, 0, 0, nis));
-          if (G == 2) {
-            const float gx = ra * dcx, gy = ra * dcy;
+          // the rotation rate 0.5 ((dcx sin th + vce - vcw) odx - (dcy cos th
+          // + ucn - ucs) ody) in the group's frame, as ps sin th0 + pc cos th0
+          // + p0 per direction (two multiply-adds)
+          const float ps = 0.5f * (ra * dcx * odx + rb * dcy * ody), pc = 0.5f * (rb * dcx * odx - ra * dcy * ody);
+          const float p0 = 0.5f * ((vce - vcw) * odx - (ucn - ucs) * ody);
 #pragma unroll
-            for (int k = 0; k < H; ++k) {
-              const float rr = 0.5f * ((gx * prm.sth[k] + vce - vcw) * odx - (gy * prm.cth[k] + ucn - ucs) * ody);
-              rmx = fmaxf(rmx, rr);
-            }
-          } else {
-            // dcx sin th - dcy cos th in the group's frame
-            const float ps = 0.5f * (ra * dcx * odx + rb * dcy * ody), pc = 0.5f * (rb * dcx * odx - ra * dcy * ody);
-            const float p0 = 0.5f * ((vce - vcw) * odx - (ucn - ucs) * ody);
-#pragma unroll
-            for (int k = 0; k < H; ++k) rmx = fmaxf(rmx, ps * prm.sth[k] + pc * prm.cth[k] + p0);
-          }
+          for (int k = 0; k < H; ++k) rmx = fmaxf(rmx, fmaf(ps, prm.sth[k], fmaf(pc, prm.cth[k], p0)));
         }
       }
       const float hk = Lc.k3dk * hdth;
