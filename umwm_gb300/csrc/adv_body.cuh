@@ -304,11 +304,8 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
       aln = alp; ben = bep;
     }
     auto rot = [&](int k, float al, float be) { return al * prm.sth[k] + (be * prm.cth[k] + c0); };
-    float rr = 0.f, rcur = 0.f;
-    if (refr) {
-      rcur = rot(0, alc, bec);
-      rr = 0.5f * (rcur + rot(H - 1, alp, bep));
-    }
+    float rr = 0.f, fprev = 0.f;  // the rate and the flux of the edge before direction 0
+    if (refr) rr = 0.5f * (rot(0, alc, bec) + rot(H - 1, alp, bep));
     const float U = wi.wspd + wi.ustar25 * __ldg(T + tS + T_LOGL2Z * 32);
     const float cp0 = __ldg(T + tS + T_CP0 * 32), fkovg = __ldg(T + tS + T_FKOVG * 32);
     const float kdk = __ldg(T + tS + T_KDK * 32);
@@ -400,17 +397,20 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
                                 : (h == 0 ? lde(ESo + oPt + pprev * 32) : lde(ESo + oS + (k0 - 1) * 32));
           const float esR = TMA ? (h == NPART - 1 ? ownES[sPt + pnext * 32] : ownES[sS + (k0 + HH) * 32])
                                 : (h == NPART - 1 ? lde(ESo + oPt + pnext * 32) : lde(ESo + oS + (k0 + HH) * 32));
+          // the flux through the edge between k and k+1, F(k) = max(rl, 0)
+          // e(k) + min(rl, 0) e(k+1), with rl the edge's rotation rate (the
+          // mean of the two directions' rates, from the edge's mean sin and
+          // cos); each direction takes F(k) - F(k-1), and F(k) carries on
+          if (h == 0) fprev = fmaxf(rr, 0.f) * esL + fminf(rr, 0.f) * es[0];
 #pragma unroll
           for (int i = 0; i < HH; ++i) {
             const int k = k0 + i;
-            const float rnext = (k + 1 < H) ? rot(k + 1, alc, bec) : rot(0, aln, ben);
-            const float rl = 0.5f * (rcur + rnext);
+            const float rl = (k + 1 < H) ? fmaf(alc, prm.shs[k], fmaf(bec, prm.chs[k], c0))
+                                         : 0.5f * (rot(H - 1, alc, bec) + rot(0, aln, ben));
             const float el = (i + 1 < HH) ? es[i + 1] : esR;
-            const float er = (i > 0) ? es[i - 1] : esL;
-            const float fl = fmaxf(rl, 0.f) * es[i] + fminf(rl, 0.f) * el - fmaxf(rr, 0.f) * er - fminf(rr, 0.f) * es[i];
-            ef[i] = ef[i] - dtrq * fl;
-            rr = rl;
-            rcur = rnext;
+            const float fk = fmaxf(rl, 0.f) * es[i] + fminf(rl, 0.f) * el;
+            ef[i] = ef[i] - dtrq * (fk - fprev);
+            fprev = fk;
           }
         }
         if (ice) {

@@ -100,6 +100,7 @@ struct Params {
   int phys_tma;      // the dts pre-pass does (k_source_tma; option "phys_tma")
   float f[MAX_OM], dom[MAX_OM];
   float th[MAX_PM], cth[MAX_PM], sth[MAX_PM], c2th[MAX_PM], s2th[MAX_PM];
+  float shs[MAX_PM], chs[MAX_PM];  // (sin th(p) + sin th(p+1)) / 2, the same for cos: the edge between p and p+1
   // max(cos th, 0), min(cos th, 0), max(sin th, 0), min(sin th, 0): the
   // upwind weights of propagation (umwm_advection.F90:34-47)
   float cthp[MAX_PM], cthm[MAX_PM], sthp[MAX_PM], sthm[MAX_PM];

@@ -628,6 +628,9 @@ int setup_params(Model& M) {
   for (int q = 0; q < H.pm; ++q) {
     p.th[q] = H.th[q]; p.cth[q] = H.cth[q]; p.sth[q] = H.sth[q];
     p.cthp[q] = std::max(H.cth[q], 0.f); p.cthm[q] = std::min(H.cth[q], 0.f);
+    const int q1 = (q + 1) % H.pm;
+    p.shs[q] = 0.5f * (H.sth[q] + H.sth[q1]);
+    p.chs[q] = 0.5f * (H.cth[q] + H.cth[q1]);
     p.sthp[q] = std::max(H.sth[q], 0.f); p.sthm[q] = std::min(H.sth[q], 0.f);
     p.c2th[q] = (float)std::cos(2.0 * (double)H.th[q]);
     p.s2th[q] = (float)std::sin(2.0 * (double)H.th[q]);
