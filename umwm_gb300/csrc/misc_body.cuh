@@ -8,6 +8,26 @@
 
 namespace umwm {
 
+// The cut-off index oc: the largest o <= O - 2 with f(o) < fc (1-based f),
+// else 1 (umwm_source_functions.F90:25-36), by bisection over the
+// increasing frequencies (the same index as the reference's downward scan)
+__device__ __forceinline__ int cutoff_level(const Params& prm, float fc) {
+  int a = -1, b = prm.O - 3;  // 0-based: the largest i in [0, O - 3] with f[i] < fc, or -1
+  while (a < b) {
+    const int m = (a + b + 1) >> 1;
+    if (prm.f[m] < fc) a = m;
+    else b = m - 1;
+  }
+  return a >= 0 ? a + 1 : 1;
+}
+
+// ctl->anycurrent = 1 where cur holds, one store per warp (every lane of
+// the warp's active set calls this)
+__device__ __forceinline__ void set_anycurrent(Ctl* ctl, bool cur) {
+  const unsigned act = __activemask();
+  if (__any_sync(act, cur) && (threadIdx.x & 31) == __ffs(act) - 1) ctl->anycurrent = 1;
+}
+
 // One all-point index i of member M (its forcing interpolation at sumt; for
 // wet points also oc, oc_rot and the sheltering coefficient): the per-stage
 // kernel's form, one point per thread (0.13 ms at 1000x1000, against 0.27
@@ -41,17 +61,13 @@ __device__ __forceinline__ void prep_point(const Params& prm, const Ptrs& P, con
   P.rhorat[ia] = P.rhoa[ia] / P.rhow[ia];
   const float ws = fmaxf(P.wspd[ia], 1e-2f);
   P.wspd[ia] = ws;
-  if ((prm.isglobal || i < M.N) && (P.uc[ia] != 0.f || P.vc[ia] != 0.f)) ctl->anycurrent = 1;
+  set_anycurrent(ctl, (prm.isglobal || i < M.N) && (P.uc[ia] != 0.f || P.vc[ia] != 0.f));
   if (i < M.N) {
     const int j = M.off + i;
     float fc = 0.53f * prm.g / ws;
     if (fc > prm.fprog) fc = prm.fprog;
     P.fcutoff[j] = fc;
-    int oc = 1;
-    for (int o = prm.O - 2; o >= 1; --o) {
-      oc = o;
-      if (fc > prm.f[o - 1]) break;
-    }
+    const int oc = cutoff_level(prm, fc);
     P.oc[j] = oc;
     if (compute_rot) P.oc_rot[j] = oc;
     P.shelt[j] = shelter_coare35(ws);
@@ -126,17 +142,13 @@ __device__ __forceinline__ void prep_finish(const Params& prm, const Ptrs& P, co
   P.rhorat[ia] = rhoa / rhow;
   const float ws = fmaxf(wspd, 1e-2f);
   P.wspd[ia] = ws;
-  if ((prm.isglobal || i < M.N) && (uc != 0.f || vc != 0.f)) ctl->anycurrent = 1;
+  set_anycurrent(ctl, (prm.isglobal || i < M.N) && (uc != 0.f || vc != 0.f));
   if (i < M.N) {
     const int j = M.off + i;
     float fc = 0.53f * prm.g / ws;
     if (fc > prm.fprog) fc = prm.fprog;
     P.fcutoff[j] = fc;
-    int oc = 1;
-    for (int o = prm.O - 2; o >= 1; --o) {
-      oc = o;
-      if (fc > prm.f[o - 1]) break;
-    }
+    const int oc = cutoff_level(prm, fc);
     P.oc[j] = oc;
     if (compute_rot) P.oc_rot[j] = oc;
     P.shelt[j] = shelter_coare35(ws);
