@@ -424,9 +424,14 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
       for (int i = 0; i < HH; ++i) {
         const int k = k0 + i;
         if (CNT) ncut += (valid && ef[i] < 0.f) ? 1 : 0;
-        ef[i] = ef[i] < 0.f ? 0.f : ef[i];  // NaN stays NaN
+        ef[i] = max_nan0(ef[i]);  // NaN stays NaN
         if (valid && prog) Eo[oS + k * 32] = ef[i];
-        sdir[i] = sin_dir(prm, wi, U, cws[k][threadIdx.x], ucg * prm.cth[k], vcg * prm.sth[k], cp0, fkovg, !prog);
+        // Sin without the level's factor gl = c1 fkovg (>= 0), which
+        // multiplies the level's stress sums instead
+        const float cw = cws[k][threadIdx.x];
+        const float x = U * cw - cp0 - ucg * prm.cth[k] - vcg * prm.sth[k];
+        const float sf = (x * fabsf(x)) * (x > 0.f ? wi.shelt : (cw > 0.f ? prm.sin_neg2 : prm.sin_neg1));
+        sdir[i] = prog ? sf : fmaxf(sf, 0.f);
       }
       if constexpr (PKD) {  // even and odd directions summed apart
 #pragma unroll
@@ -449,8 +454,8 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
       tx += tx2.x + tx2.y;
       ty += ty2.x + ty2.y;
     }
-    tx *= ra * icp;
-    ty *= ra * icp;
+    tx *= ra * icp * (wi.c1 * fkovg);
+    ty *= ra * icp * (wi.c1 * fkovg);
     sx += tx * kdk; sy += ty * kdk;
     if (o >= oc - 1) { dsx += tx * kdk; dsy += ty * kdk; }
     if (o == O - 1) { txom = tx; tyom = ty; }

@@ -56,6 +56,13 @@ __device__ __forceinline__ WindIn load_wind(const Params& prm, const Ptrs& P, in
 // all-point index of a wet (or ghost) point of member M
 __device__ __forceinline__ int apt(const Member& M, int j) { return M.nmoff + (j - M.off); }
 
+// max(x, 0) with NaN kept (max.NaN)
+__device__ __forceinline__ float max_nan0(float x) {
+  float r;
+  asm("max.NaN.f32 %0, %1, 0f00000000;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 // Sin of one bin from x = U cos(wdir - th) - cp0 - uc cos th - vc sin th,
 // umwm_source_functions.F90:39-80, with its factors folded: the reference
 // forms sin_fac |x| x, then multiplies by shelt/sin_fac where positive, by
