@@ -96,6 +96,8 @@ struct Params {
   int minb_phys, minb_integ, minb_adv;
   int pf_phys, pf_integ, pf_adv;
   int count_cut;     // the propagation counts the bins its non-negativity cut changes (Global::cut_count)
+  int swsign;        // the first pm/2 directions have sin th < 0, and cos th < 0 exactly for the first pm/4
+                     // (pm % 4 == 0): the two-group flux takes one upwind term per slot pair
   int adv_tma;       // the propagation stages its own rows with bulk copies (k_advect_tma; option "advect_tma")
   int phys_tma;      // the dts pre-pass does (k_source_tma; option "phys_tma")
   float f[MAX_OM], dom[MAX_OM];

@@ -625,6 +625,13 @@ int setup_params(Model& M) {
     p.ice_possible |= (mh.H.seaice || (mh.H.fice0 > mh.H.fice_lth));
   }
   for (int o = 0; o < H.om; ++o) { p.f[o] = H.f[o]; p.dom[o] = H.dom[o]; }
+  // the two-group flux of pm % 4 == 0 grids takes one upwind term per slot
+  // pair (adv_body.cuh): the grid th(p) = (p - (pm + 1) / 2) dth gives the
+  // first pm/2 directions sin th < 0 and cos th < 0 exactly below pm/4
+  p.swsign = H.pm % 4 == 0;
+  for (int q = 0; q < H.pm / 2; ++q)
+    if (!(H.sth[q] < 0.f) || !(q < H.pm / 4 ? H.cth[q] < 0.f : H.cth[q] > 0.f)) p.swsign = 0;
+  if (H.pm % 4 == 0 && !p.swsign) return fail(UMWM_ERR_NAMELIST, "direction grid without the expected signs");
   for (int q = 0; q < H.pm; ++q) {
     p.th[q] = H.th[q]; p.cth[q] = H.cth[q]; p.sth[q] = H.sth[q];
     p.cthp[q] = std::max(H.cth[q], 0.f); p.cthm[q] = std::min(H.cth[q], 0.f);
