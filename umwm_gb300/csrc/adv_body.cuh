@@ -414,17 +414,18 @@ __device__ __forceinline__ void advect_body(const Params& prm, const Ptrs& P, in
           const float esR = TMA ? (h == NPART - 1 ? ownES[sPt + pnext * 32] : ownES[sS + (k0 + HH) * 32])
                                 : (h == NPART - 1 ? lde(ESo + oPt + pnext * 32) : lde(ESo + oS + (k0 + HH) * 32));
           // the flux through the edge between k and k+1, F(k) = max(rl, 0)
-          // e(k) + min(rl, 0) e(k+1), with rl the edge's rotation rate (the
-          // mean of the two directions' rates, from the edge's mean sin and
-          // cos); each direction takes F(k) - F(k-1), and F(k) carries on
-          if (h == 0) fprev = fmaxf(rr, 0.f) * esL + fminf(rr, 0.f) * es[0];
+          // e(k) + min(rl, 0) e(k+1) = rl e(upwind side), with rl the edge's
+          // rotation rate (the mean of the two directions' rates, from the
+          // edge's mean sin and cos); each direction takes F(k) - F(k-1),
+          // and F(k) carries on
+          if (h == 0) fprev = rr * (rr > 0.f ? esL : es[0]);
 #pragma unroll
           for (int i = 0; i < HH; ++i) {
             const int k = k0 + i;
             const float rl = (k + 1 < H) ? fmaf(alc, prm.shs[k], fmaf(bec, prm.chs[k], c0))
                                          : 0.5f * (rot(H - 1, alc, bec) + rot(0, aln, ben));
             const float el = (i + 1 < HH) ? es[i + 1] : esR;
-            const float fk = fmaxf(rl, 0.f) * es[i] + fminf(rl, 0.f) * el;
+            const float fk = rl * (rl > 0.f ? es[i] : el);  // the upwind side's E*
             ef[i] = ef[i] - dtrq * (fk - fprev);
             fprev = fk;
           }
